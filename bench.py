@@ -1,0 +1,396 @@
+#!/usr/bin/env python
+"""Throughput of the ForceAtlas2 iteration on GB300 (node-iterations/s).
+
+Workload (default): stochastic block model, 1,000,000 nodes in 1,000 blocks
+of power-law sizes (exponent 2.1), mean within-block degree 12, mean
+between-block degree 2 (~7M edges), unit weights; linlog + dissuade_hubs,
+Barnes-Hut theta 1.2, positions and forces in FP32, swing/traction totals
+and the speed controller in FP64. Synthetic, generated from a seed.
+
+One step = one ForceAtlas2 iteration of the whole graph (Morton codes, radix
+sort, Karras tree, Barnes-Hut repulsion, attraction and gravity, swing and
+traction, displacement), with the graph already resident in HBM. The
+iteration's working set (~0.3 GB) exceeds the 129 MB L2, so no flush is
+needed between steps.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl reference times the reference's CPU engine (src/forceatlas2.c's
+C_forceatlas2 loop with the Gephi quadtree, OpenMP on every host core; the
+oracle's restatement, since the reference sources are not on the GPU host)
+on the same workload. With N > 1 (torchrun), each rank lays out its own
+replica on its own GPU (the layouts are independent: no collective on the
+data path); value is the sum over ranks, timed by the slowest rank.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = ("node-iters/s FP32 vs FP64 at ≤1e-4 force err; served layouts/s, "
+          "p99 latency")
+UNIT = "node-iters/s"
+WORKLOAD = ("SBM n=1,000,000, 1000 power-law blocks (exp 2.1), deg_in 12, "
+            "deg_out 2, unit weights; linlog + dissuade_hubs, Barnes-Hut "
+            "theta 1.2, FP32 positions/forces, FP64 speed control")
+# kernels of one Barnes-Hut iteration: bbox, morton, 4 x (hist, scan,
+# scatter), gather, karras, aggregate, traverse, attract, swing, apply
+LAUNCHES_PER_ITER = 21
+# algorithmic HBM bytes per node of the traversal: psort record 16, order 4,
+# force write 8 (FP32)
+TRAVERSE_HBM_BYTES_PER_NODE = 28
+
+
+def make_workload(small: bool = False):
+    from forceatlas2_rc_gb300 import graphs
+    if small:
+        n, a, b = graphs.sbm(20000, 50, 2.1, 12.0, 2.0, seed=1)
+    else:
+        n, a, b = graphs.sbm(1_000_000, 1000, 2.1, 12.0, 2.0, seed=1)
+    r = 10.0 * np.sqrt(n)
+    pos = graphs.uniform_positions(n, -r, r, seed=2)
+    return n, a, b, pos
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class Clocks:
+    """nvidia-smi samples of SM clocks and throttle reasons while running."""
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.dev = device
+        self.proc = None
+        self.f = None
+
+    def __enter__(self):
+        try:
+            self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.dev), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.proc or not self.f:
+            return None
+        self.f.flush()
+        rows = []
+        with open(self.f.name) as fh:
+            for line in fh:
+                p = [x.strip() for x in line.split(",")]
+                if len(p) < 8:
+                    continue
+                try:
+                    rows.append((float(p[0]), float(p[1]), p[4:8]))
+                except ValueError:
+                    continue
+        os.unlink(self.f.name)
+        if not rows:
+            return None
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown",
+                 "sw_power_cap"]
+        reasons = sorted({names[k] for _, _, r in rows for k in range(4)
+                          if r[k].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(r[0] for r in rows),
+                "sm_max_mhz": max(r[1] for r in rows),
+                "reasons": reasons, "samples": len(rows)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except Exception:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+def cpu_sample(n, a, b, iters, threads):
+    """The reference's CPU engine (C_forceatlas2 with the quadtree) on this
+    host: node-iterations/s over `iters` iterations after one warm-up."""
+    import oracle
+    o = oracle.Opts(scaling=2.0, gravity=1.0, linlog=True, outbound=True,
+                    barnes_hut=True, theta=1.2, threads=threads)
+    r = 10.0 * np.sqrt(n)
+    from forceatlas2_rc_gb300 import graphs
+    pos = graphs.uniform_positions(n, -r, r, seed=2)
+    w = np.ones(len(a))
+    oracle.layout(n, a, b, w, pos, None, None, 1, o)
+    t0 = time.perf_counter()
+    oracle.layout(n, a, b, w, pos, None, None, iters, o)
+    dt = time.perf_counter() - t0
+    return n * iters / dt, dt
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    import oracle
+    oracle.build()
+    threads = os.cpu_count() or 1
+    n, a, b, _ = make_workload(args.small)
+    w = np.ones(len(a))
+    o = oracle.Opts(scaling=2.0, gravity=1.0, linlog=True, outbound=True,
+                    barnes_hut=True, theta=1.2, threads=threads)
+    r = 10.0 * np.sqrt(n)
+    from forceatlas2_rc_gb300 import graphs
+    pos = graphs.uniform_positions(n, -r, r, seed=2)
+    pos = oracle.layout(n, a, b, w, pos, None, None, args.warmup, o)
+    t0 = time.perf_counter()
+    oracle.layout(n, a, b, w, pos, None, None, args.steps, o)
+    dt = time.perf_counter() - t0
+    value = n * args.steps / dt
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
+        "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1000.0 * dt / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic",
+        "config": {"workload": WORKLOAD, "n": n, "edges": int(len(a)),
+                   "engine": "src/forceatlas2.c C_forceatlas2 loop (quadtree "
+                             "Barnes-Hut, OpenMP), oracle restatement"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads,
+                         "kind": "port",
+                         "sample": f"{args.steps} iterations of the full "
+                                   f"workload after {args.warmup} warm-up"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--small", action="store_true",
+                    help="20000-node SBM (quick check, not a bench line)")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--profile-only", action="store_true",
+                    help="warm-up and a few iterations only (for ncu)")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    ws, rank, local = dist_env()
+    import torch
+    torch.cuda.set_device(local)
+    pg = None
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+        pg = dist
+
+    from forceatlas2_rc_gb300 import build as fbuild
+    fbuild.build()
+    from forceatlas2_rc_gb300 import _lib
+    from forceatlas2_rc_gb300._abi import FA2_FULL_NTIMES, dptr
+    from forceatlas2_rc_gb300.layout import REPULSION_BH, Graph, Layout, _params
+
+    n, a, b, pos = make_workload(args.small)
+    g = Graph(n, a, b, np.ones(len(a)), outbound=True)
+    kw = dict(scaling=2.0, gravity=1.0, theta=1.2, linlog=True, device=local)
+    L = Layout(g, pos, precision="single", repulsion=REPULSION_BH, **kw)
+    stream = torch.cuda.ExternalStream(L.stream, device=local)
+
+    if args.profile_only:
+        L.iterate(max(args.warmup, 1))
+        L.sync()
+        L.close()
+        return 0
+
+    L.iterate(args.warmup)
+    L.sync()
+
+    # ---- value: device-resident throughput --------------------------------
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    if pg:
+        pg.barrier()
+    torch.cuda.synchronize()
+    with Clocks(local) as clk:
+        ev0.record(stream)
+        L.iterate(args.steps)
+        ev1.record(stream)
+        ev1.synchronize()
+    L.sync()
+    ms = ev0.elapsed_time(ev1)
+    torch.cuda.synchronize()
+    if pg:
+        t = torch.tensor([ms], device=f"cuda:{local}")
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        ms = float(t.item())
+        pg.barrier()
+    clocks = clk.summary()
+    value = ws * n * args.steps / (ms / 1000.0)
+
+    # ---- phase times (CUDA events on the layout's stream) -----------------
+    ph = L.phase_times(10)
+    ph = {k: v / 10.0 for k, v in ph.items()}
+    counts = L.traversal_counts()
+
+    # ---- FP32 vs FP64: force error and same-GPU FP64 throughput -----------
+    xy = L.positions()
+    f32 = L.forces(xy)
+    L.close()
+    L64 = Layout(g, xy, precision="double", repulsion=REPULSION_BH, **kw)
+    f64 = L64.forces(xy)
+    den = np.sqrt((f64 ** 2).sum(1)).max()
+    force_err = float(np.sqrt(((f32 - f64) ** 2).sum(1)).max() / den)
+    L64.set_positions(xy)
+    L64.iterate(2)
+    L64.sync()
+    k64 = max(3, args.steps // 10)
+    s64 = torch.cuda.ExternalStream(L64.stream, device=local)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(s64)
+    L64.iterate(k64)
+    e1.record(s64)
+    e1.synchronize()
+    L64.sync()
+    fp64_value = n * k64 / (e0.elapsed_time(e1) / 1000.0)
+    L64.close()
+
+    # ---- e2e: fa2_full_run (the C interface the package calls) with host
+    #      buffers in pinned memory; each step = one whole layout of 1000
+    #      iterations, uploads and download included -------------------------
+    e2e = None
+    if not args.no_e2e:
+        import ctypes as C
+
+        def pinned(arr):
+            t = torch.empty(arr.shape, dtype=getattr(torch, str(arr.dtype)),
+                            pin_memory=True)
+            out = t.numpy()
+            out[...] = arr
+            return out, t
+
+        keep = []
+        host = {}
+        for k2, arr in (("inc_off", g.inc_off), ("inc_node", g.inc_node),
+                        ("inc_coef", g.inc_coef), ("mass", g.mass),
+                        ("size", np.ones(n)), ("fixed", np.zeros(n, np.int32)),
+                        ("pos", np.ascontiguousarray(pos.T.reshape(-1)))):
+            host[k2], t = pinned(np.ascontiguousarray(arr))
+            keep.append(t)
+        g2 = Graph.__new__(Graph)
+        g2.n, g2.mass = n, host["mass"]
+        g2.inc_off, g2.inc_node, g2.inc_coef = host["inc_off"], host["inc_node"], host["inc_coef"]
+        iters = 1000
+        p, keep2 = _params(g2, host["size"], host["fixed"], 2.0, 1.0, 1.2, 1.0,
+                           False, True, False, iters, local, False)
+        times = np.zeros(FA2_FULL_NTIMES)
+        lib = _lib.load()
+        xy0 = host["pos"].copy()
+        calls = 2
+        h2d = sum(host[k2].nbytes for k2 in ("inc_off", "inc_node", "inc_coef",
+                                             "mass", "pos"))
+        d2h = host["pos"].nbytes
+        # warm-up call
+        host["pos"][:] = xy0
+        assert lib.fa2_full_run(C.byref(p), dptr(host["pos"]), dptr(times)) == 0, _lib.error()
+        if pg:
+            pg.barrier()
+        t0 = time.perf_counter()
+        for _ in range(calls):
+            host["pos"][:] = xy0
+            rc = lib.fa2_full_run(C.byref(p), dptr(host["pos"]), dptr(times))
+            assert rc == 0, _lib.error()
+        dt = time.perf_counter() - t0
+        if pg:
+            t = torch.tensor([dt], device=f"cuda:{local}")
+            pg.all_reduce(t, op=pg.ReduceOp.MAX)
+            dt = float(t.item())
+        e2e = {"value": ws * n * iters * calls / dt, "unit": UNIT,
+               "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+               "step": "fa2_full_run, 1000 iterations, host buffers (pinned)",
+               "s_per_layout": dt / calls}
+
+    # ---- roofline of the dominant kernel (the traversal) -------------------
+    peaks, kind = measured_peaks()
+    t_trav = ph["repulsion"] / 1000.0
+    alg = TRAVERSE_HBM_BYTES_PER_NODE * n
+    achieved = alg / t_trav / 1e9
+    l2_bytes = 32.0 * counts["visits"] + 16.0 * counts["pairs"]
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"],
+                "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"],
+                "traffic": None, "kernel": "k_traverse<float>",
+                "peak_kind": f"{kind} (HBM copy)",
+                "launch_ms": ph["repulsion"],
+                "l2_request_bytes": l2_bytes,
+                "l2_request_gbs": l2_bytes / t_trav / 1e9,
+                "visits_per_node": counts["visits"] / n,
+                "pairs_per_node": counts["pairs"] / n}
+
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu:
+        threads = os.cpu_count() or 1
+        cv, cdt = cpu_sample(n, a, b, 3, threads)
+        cpu = {"value": cv, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"3 iterations of the full {n}-node workload (after 1 "
+                         f"warm-up), C_forceatlas2 quadtree engine, {cdt:.1f} s"}
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": WORKLOAD, "n": n, "edges": int(len(a)),
+                   "parallelism": "replicas" if ws > 1 else "single GPU",
+                   "l2": "working set > 129 MB L2 (no flush needed)"},
+        "fp64_value": fp64_value,
+        "fp32_over_fp64": value / ws / fp64_value,
+        "force_err_fp32_vs_fp64": force_err,
+        "iterations_per_s": 1000.0 * args.steps / ms,
+        "phase_ms": ph,
+        "gpu_launches": LAUNCHES_PER_ITER * args.steps,
+        "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu,
+        "clocks": clocks,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if pg:
+        pg.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,89 @@
+// common.cuh -- shared definitions of libfa2cuda.so: error reporting, the
+// real-number traits of the two precisions, device helpers.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/fa2.h"
+#include "../../include/fa2_cuda.h"
+
+namespace fa2cu {
+
+// ---- errors (the fa2_gpu_error() buffer, reference src/gpu.c:129-143) ----
+void set_message(const char *fmt, ...);
+void set_cuda_error(const char *what, cudaError_t e);
+// The CUDA call of the expression, on failure: message and return `ret`.
+#define FA2_TRY(expr, what, ret)                                               \
+    do {                                                                       \
+        cudaError_t e_ = (expr);                                               \
+        if (e_ != cudaSuccess) {                                               \
+            ::fa2cu::set_cuda_error(what, e_);                                 \
+            return ret;                                                        \
+        }                                                                      \
+    } while (0)
+
+// Device-side status words (one int each in a session's `status` buffer).
+enum {
+    ST_ERROR = 0,      // non-zero: a kernel gave up; bit values below
+    ST_TICKET_BBOX,    // arrival counters of the last-block reductions
+    ST_TICKET_SWING,
+    ST_TICKET_NODE,
+    ST_COUNT
+};
+enum {
+    ERR_NAN = 1,       // swing/traction totals were not numbers
+    ERR_WAIT = 2,      // a bounded wait on an mbarrier ran out
+    ERR_BOUNDS = 4,    // a computed index or walk left its bounds (a bug)
+};
+
+// Speed-controller state on the device, in double (reference
+// src/forceatlas2.c:445-485 runs it on the host; here it never leaves HBM).
+struct SpeedState {
+    double speed, efficiency;
+    double total_swinging, total_traction;
+    double jitter_tolerance;
+    int n, pad;
+};
+
+// ---- precision traits -----------------------------------------------------
+template <class R> struct RT;
+template <> struct RT<float> {
+    typedef float2 R2;
+    typedef float4 R4;
+};
+template <> struct RT<double> {
+    typedef double2 R2;
+    typedef double4_32a R4;
+};
+
+// Tree-node record of the Barnes-Hut traversal: centre of mass, mass and
+// squared size, then the left child, the next node that is not a descendant
+// (-1 at the end) and the range of sorted nodes covered. 32 bytes in float,
+// 64 in double; one record per internal node of the Karras tree.
+template <class R> struct alignas(sizeof(R) * 4 >= 32 ? 64 : 32) BHNode {
+    typename RT<R>::R4 c;  // cx, cy, m, size^2
+    int4 t;                // left, skip, first, last
+};
+
+// One CSR incidence: the node at the other end and the attraction strength.
+template <class R> struct alignas(2 * sizeof(R) > 8 ? 16 : 8) Inc {
+    int j;
+    R coef;
+};
+
+// Per-node sum over the internal nodes of the tree (bbox, mass, m*x, m*y).
+template <class R> struct alignas(sizeof(R) * 8) Agg {
+    R minx, miny, maxx, maxy, m, mx, my, pad;
+};
+
+// Leaves of a device-side quadtree region list (fa2_gpu_repulse_bh):
+// rr = (cx, cy, mass, size^2), ri = (start, count, last child, skip).
+template <class R> struct QRegion {
+    typename RT<R>::R4 rr;
+    int4 ri;
+};
+
+inline int ceil_div(long long a, long long b) { return (int) ((a + b - 1) / b); }
+
+} // namespace fa2cu

@@ -1,0 +1,16 @@
+// inst_f32.cu -- the FP32 path: every kernel of kernels.cuh instantiated for
+// float. Built with FMA contraction and approximate division / square root
+// (-ftz=true -prec-div=false -prec-sqrt=false); the steps that must be
+// bit-exact use explicit round-to-nearest intrinsics.
+#include "layout_impl.cuh"
+
+namespace fa2cu {
+LayoutBase *make_layout_f32(const fa2_full_params *p, const double *pos, int rep)
+{
+    return make_layout<float>(p, pos, rep);
+}
+RepulseBase *make_repulse_f32(int device, int n, int adjust, int bh)
+{
+    return make_repulse<float>(device, n, adjust, bh);
+}
+} // namespace fa2cu

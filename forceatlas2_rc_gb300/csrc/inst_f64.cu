@@ -1,0 +1,16 @@
+// inst_f64.cu -- the FP64 path (precision = "double"): every kernel of
+// kernels.cuh instantiated for double, built with -fmad=false and IEEE
+// division and square root so that each force is computed with the
+// operations, in the order, of the reference's src/forceatlas2.c.
+#include "layout_impl.cuh"
+
+namespace fa2cu {
+LayoutBase *make_layout_f64(const fa2_full_params *p, const double *pos, int rep)
+{
+    return make_layout<double>(p, pos, rep);
+}
+RepulseBase *make_repulse_f64(int device, int n, int adjust, int bh)
+{
+    return make_repulse<double>(device, n, adjust, bh);
+}
+} // namespace fa2cu

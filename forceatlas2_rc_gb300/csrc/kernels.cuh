@@ -1,0 +1,910 @@
+// kernels.cuh -- the per-iteration ForceAtlas2 kernels, templated on the
+// real type. inst_f32.cu instantiates them for float (FMA contraction, fast
+// division and square root: the FP32 path), inst_f64.cu for double with
+// -fmad=false and IEEE division (the FP64 path, which keeps the operation
+// order of the reference so that it reproduces src/forceatlas2.c).
+//
+// Steps that must be bit-exact in both precisions (Morton codes, centres of
+// mass) use the explicit round-to-nearest intrinsics, which are never fused.
+#pragma once
+
+#include "common.cuh"
+
+namespace fa2cu {
+
+// ---- arithmetic helpers ---------------------------------------------------
+
+__device__ __forceinline__ float radd(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float rsub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ float rmul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float rdiv(float a, float b) { return __fdiv_rn(a, b); }
+__device__ __forceinline__ double radd(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double rsub(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ double rmul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double rdiv(double a, double b) { return __ddiv_rn(a, b); }
+
+// Division and square root of the hot loops: approximate in float (2 ulp),
+// IEEE in double.
+__device__ __forceinline__ float fdiv(float a, float b) { return __fdividef(a, b); }
+__device__ __forceinline__ double fdiv(double a, double b) { return a / b; }
+__device__ __forceinline__ float fsqrt(float a) { return sqrtf(a); }
+__device__ __forceinline__ double fsqrt(double a) { return sqrt(a); }
+__device__ __forceinline__ float flog1p(float a) { return log1pf(a); }
+__device__ __forceinline__ double flog1p(double a) { return log1p(a); }
+
+// OpenCL min / max of the reference (pipeline.cl), exact.
+template <class R> __device__ __forceinline__ R cl_min(R a, R b) { return b < a ? b : a; }
+template <class R> __device__ __forceinline__ R cl_max(R a, R b) { return a < b ? b : a; }
+
+template <class R> __device__ __forceinline__ typename RT<R>::R2 mk2(R a, R b)
+{
+    typename RT<R>::R2 v;
+    v.x = a;
+    v.y = b;
+    return v;
+}
+template <class R>
+__device__ __forceinline__ typename RT<R>::R4 mk4(R a, R b, R c, R d)
+{
+    typename RT<R>::R4 v;
+    v.x = a;
+    v.y = b;
+    v.z = c;
+    v.w = d;
+    return v;
+}
+
+// Repulsion factor between two nodes (reference src/forceatlas2.c:265-275,
+// pipeline.cl:46-55): the force on the first is (xd, yd) * factor.
+template <class R, bool ADJUST>
+__device__ __forceinline__ R rep_factor(R d2, R mm, R ss, R scaling)
+{
+    if (ADJUST) {
+        const R d = fsqrt(d2) - ss;
+        if (d > R(0)) return fdiv(scaling * mm, d * d);
+        if (d < R(0)) return R(100) * scaling * mm;
+        return R(0);
+    }
+    return d2 > R(0) ? fdiv(scaling * mm, d2) : R(0);
+}
+
+// ---- block reductions -----------------------------------------------------
+
+template <class T> __device__ __forceinline__ T warp_sum(T v)
+{
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// ---- 1. bounding box (pipeline.cl:61-99) ----------------------------------
+// Block partial minima / maxima, then the last block to finish reduces the
+// partials: min and max are exact, so the result does not depend on order.
+template <class R>
+__global__ void __launch_bounds__(256)
+k_bbox(int n, const typename RT<R>::R2 *__restrict__ pos, R *__restrict__ partial,
+       R *__restrict__ bbox, unsigned *__restrict__ ticket)
+{
+    typedef typename RT<R>::R2 R2;
+    R mnx, mny, mxx, mxy;
+    {
+        const R2 p0 = pos[0];
+        mnx = mxx = p0.x;
+        mny = mxy = p0.y;
+    }
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += gridDim.x * blockDim.x) {
+        const R2 p = pos[i];
+        mnx = cl_min(mnx, p.x);
+        mny = cl_min(mny, p.y);
+        mxx = cl_max(mxx, p.x);
+        mxy = cl_max(mxy, p.y);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        mnx = cl_min(mnx, __shfl_down_sync(0xffffffffu, mnx, o));
+        mny = cl_min(mny, __shfl_down_sync(0xffffffffu, mny, o));
+        mxx = cl_max(mxx, __shfl_down_sync(0xffffffffu, mxx, o));
+        mxy = cl_max(mxy, __shfl_down_sync(0xffffffffu, mxy, o));
+    }
+    __shared__ R s[4][8];
+    __shared__ int last;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (lane == 0) {
+        s[0][w] = mnx;
+        s[1][w] = mny;
+        s[2][w] = mxx;
+        s[3][w] = mxy;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const int nw = blockDim.x >> 5;
+        for (int k = 1; k < nw; k++) {
+            mnx = cl_min(mnx, s[0][k]);
+            mny = cl_min(mny, s[1][k]);
+            mxx = cl_max(mxx, s[2][k]);
+            mxy = cl_max(mxy, s[3][k]);
+        }
+        R *o = partial + 4 * blockIdx.x;
+        o[0] = mnx;
+        o[1] = mny;
+        o[2] = mxx;
+        o[3] = mxy;
+        __threadfence();
+        last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!last) return;
+    if (threadIdx.x == 0) {
+        __threadfence();
+        R a = __ldcg(partial), b = __ldcg(partial + 1), c = __ldcg(partial + 2),
+          d = __ldcg(partial + 3);
+        for (int k = 1; k < (int) gridDim.x; k++) {
+            a = cl_min(a, __ldcg(partial + 4 * k));
+            b = cl_min(b, __ldcg(partial + 4 * k + 1));
+            c = cl_max(c, __ldcg(partial + 4 * k + 2));
+            d = cl_max(d, __ldcg(partial + 4 * k + 3));
+        }
+        bbox[0] = a;
+        bbox[1] = b;
+        bbox[2] = c;
+        bbox[3] = d;
+        *ticket = 0u;
+    }
+}
+
+// ---- 2. Morton codes (pipeline.cl:105-130) ---------------------------------
+
+__device__ __forceinline__ uint32_t spread16(uint32_t v)
+{
+    v &= 0xFFFFu;
+    v = (v | (v << 8)) & 0x00FF00FFu;
+    v = (v | (v << 4)) & 0x0F0F0F0Fu;
+    v = (v | (v << 2)) & 0x33333333u;
+    v = (v | (v << 1)) & 0x55555555u;
+    return v;
+}
+
+template <class R>
+__global__ void __launch_bounds__(256)
+k_morton(int n, const typename RT<R>::R2 *__restrict__ pos, const R *__restrict__ bbox,
+         uint32_t *__restrict__ key, uint32_t *__restrict__ idx)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const R minx = bbox[0], miny = bbox[1];
+    const R w = rsub(bbox[2], minx), h = rsub(bbox[3], miny);
+    const R extent = cl_max(w, h);
+    const R scale = extent > R(0) ? rdiv(R(65535), extent) : R(0);
+    const typename RT<R>::R2 p = pos[i];
+    const R fx = cl_min(cl_max(rmul(rsub(p.x, minx), scale), R(0)), R(65535));
+    const R fy = cl_min(cl_max(rmul(rsub(p.y, miny), scale), R(0)), R(65535));
+    key[i] = spread16((uint32_t) fx) | (spread16((uint32_t) fy) << 1);
+    idx[i] = (uint32_t) i;
+}
+
+// ---- 4a. nodes in sorted order (pipeline.cl:195-207) -----------------------
+
+template <class R>
+__global__ void __launch_bounds__(256)
+k_gather(int n, int adjust, const uint32_t *__restrict__ order,
+         const typename RT<R>::R2 *__restrict__ pos, const R *__restrict__ mass,
+         const R *__restrict__ size, typename RT<R>::R4 *__restrict__ psort,
+         int *__restrict__ status)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const uint32_t i = order[k];
+    if (i >= (uint32_t) n) { // never for a valid sort
+        atomicOr(status + ST_ERROR, ERR_BOUNDS);
+        psort[k] = mk4<R>(R(0), R(0), R(0), R(0));
+        return;
+    }
+    const typename RT<R>::R2 p = pos[i];
+    psort[k] = mk4<R>(p.x, p.y, mass[i], adjust ? size[i] : R(0));
+}
+
+// ---- 4c. bottom-up centres of mass (pipeline.cl:272-323) -------------------
+// One thread per leaf climbs the tree; at each region, the first child to
+// arrive stops and the second computes the region from both children
+// (fixed order a then b: the sums do not depend on who arrives last). No
+// thread ever waits. The region's traversal record gets its skip link:
+// rope[last] is the right child of the region split just after `last`.
+
+template <class R>
+__device__ __forceinline__ Agg<R> leaf_agg(const typename RT<R>::R4 &p)
+{
+    Agg<R> a;
+    a.minx = a.maxx = p.x;
+    a.miny = a.maxy = p.y;
+    a.m = p.z;
+    a.mx = rmul(p.x, p.z);
+    a.my = rmul(p.y, p.z);
+    a.pad = R(0);
+    return a;
+}
+
+template <class R>
+__device__ __forceinline__ Agg<R> load_agg_cg(const Agg<R> *a)
+{
+    Agg<R> v;
+    const R *p = reinterpret_cast<const R *>(a);
+    v.minx = __ldcg(p);
+    v.miny = __ldcg(p + 1);
+    v.maxx = __ldcg(p + 2);
+    v.maxy = __ldcg(p + 3);
+    v.m = __ldcg(p + 4);
+    v.mx = __ldcg(p + 5);
+    v.my = __ldcg(p + 6);
+    v.pad = R(0);
+    return v;
+}
+
+template <class R>
+__global__ void __launch_bounds__(256)
+k_aggregate(int n, const typename RT<R>::R4 *__restrict__ psort,
+            const int2 *__restrict__ child, const int *__restrict__ parent,
+            const int2 *__restrict__ range, const int *__restrict__ rope,
+            int *__restrict__ visits, Agg<R> *__restrict__ agg,
+            BHNode<R> *__restrict__ nodes, int *__restrict__ status)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const int nl = n - 1;
+    int r = parent[nl + k];
+    // a Karras tree over 32-bit keys and n < 2^27 nodes is < 64 levels deep
+    for (int depth = 0; r >= 0; depth++) {
+        if (r >= nl || depth > 160) {
+            atomicOr(status + ST_ERROR, ERR_BOUNDS);
+            return;
+        }
+        __threadfence();
+        if (atomicAdd(&visits[r], 1) == 0) return;
+        __threadfence();
+        const int2 c = child[r];
+        if (c.x < 0 || c.y < 0 || c.x >= nl + n || c.y >= nl + n) {
+            atomicOr(status + ST_ERROR, ERR_BOUNDS);
+            return;
+        }
+        const Agg<R> a = c.x >= nl ? leaf_agg<R>(psort[c.x - nl]) : load_agg_cg(agg + c.x);
+        const Agg<R> b = c.y >= nl ? leaf_agg<R>(psort[c.y - nl]) : load_agg_cg(agg + c.y);
+        Agg<R> q;
+        q.minx = cl_min(a.minx, b.minx);
+        q.miny = cl_min(a.miny, b.miny);
+        q.maxx = cl_max(a.maxx, b.maxx);
+        q.maxy = cl_max(a.maxy, b.maxy);
+        q.m = radd(a.m, b.m);
+        q.mx = radd(a.mx, b.mx);
+        q.my = radd(a.my, b.my);
+        q.pad = R(0);
+        agg[r] = q;
+        const R w = rsub(q.maxx, q.minx), h = rsub(q.maxy, q.miny);
+        const int2 rg = range[r];
+        BHNode<R> nd;
+        nd.c = mk4<R>(rdiv(q.mx, q.m), rdiv(q.my, q.m), q.m,
+                      rmul(R(2), radd(rmul(w, w), rmul(h, h))));
+        nd.t = make_int4(c.x, rope[rg.y], rg.x, rg.y);
+        nodes[r] = nd;
+        r = parent[r];
+    }
+}
+
+// ---- 5. Barnes-Hut traversal (pipeline.cl:329-383) -------------------------
+// One thread per node, in sorted order; the walk is stackless: from a region
+// the thread goes down to the left child or jumps to the region's skip link,
+// which visits the regions in exactly the order of the reference's stack
+// (left child first). A small region that is too close is summed node by
+// node; each step of the loop handles either one region or one node pair, so
+// the threads of a warp stay in step.
+
+template <class R, bool ADJUST>
+__global__ void __launch_bounds__(256)
+k_traverse(int n, R scaling, R theta2, const typename RT<R>::R4 *__restrict__ psort,
+           const BHNode<R> *__restrict__ nodes, const int *__restrict__ rope,
+           const uint32_t *__restrict__ order, typename RT<R>::R2 *__restrict__ f,
+           int *__restrict__ status)
+{
+    typedef typename RT<R>::R4 R4;
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const R4 me = psort[k];
+    const R xi = me.x, yi = me.y, mi = me.z, si = me.w;
+    R ax = R(0), ay = R(0);
+    const int nl = n - 1;
+    int cur = 0, j = 0, jend = -1;
+    // a walk visits each of the 2n-1 tree nodes and each node pair at most
+    // once: more steps than that, or an index out of range, is a bug
+    const int cap = 4 * n + 64;
+    for (int step = 0;; step++) {
+        if (step > cap || cur >= nl + n || jend >= n) {
+            atomicOr(status + ST_ERROR, ERR_BOUNDS);
+            break;
+        }
+        if (j <= jend) {
+            if (j != k) {
+                const R4 q = psort[j];
+                const R xd = xi - q.x, yd = yi - q.y;
+                const R g = rep_factor<R, ADJUST>(xd * xd + yd * yd, mi * q.z,
+                                                  si + q.w, scaling);
+                ax += xd * g;
+                ay += yd * g;
+            }
+            ++j;
+            continue;
+        }
+        if (cur < 0) break;
+        if (cur >= nl) { // a single node
+            j = jend = cur - nl;
+            cur = rope[j];
+            continue;
+        }
+        const BHNode<R> nd = nodes[cur];
+        const R xd = xi - nd.c.x, yd = yi - nd.c.y;
+        const R d2 = xd * xd + yd * yd;
+        if (d2 * theta2 > nd.c.w) {
+            const R g = fdiv(scaling * (mi * nd.c.z), d2);
+            ax += xd * g;
+            ay += yd * g;
+            cur = nd.t.y;
+        } else if (nd.t.w - nd.t.z >= 8) {
+            cur = nd.t.x;
+        } else {
+            j = nd.t.z;
+            jend = nd.t.w;
+            cur = nd.t.y;
+        }
+    }
+    f[order[k]] = mk2<R>(ax, ay);
+}
+
+// Instrumented copy of the walk: counts regions visited and node pairs
+// computed (for the traffic estimate of the roofline; never timed).
+template <class R>
+__global__ void __launch_bounds__(256)
+k_traverse_count(int n, R theta2, const typename RT<R>::R4 *__restrict__ psort,
+                 const BHNode<R> *__restrict__ nodes, const int *__restrict__ rope,
+                 unsigned long long *__restrict__ counts)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    unsigned long long visits = 0, pairs = 0;
+    if (k < n) {
+        const typename RT<R>::R4 me = psort[k];
+        const int nl = n - 1;
+        int cur = 0;
+        for (int step = 0; cur >= 0 && cur < nl + n && step <= 4 * n + 64; step++) {
+            if (cur >= nl) {
+                pairs += (cur - nl != k);
+                cur = rope[cur - nl];
+                continue;
+            }
+            ++visits;
+            const BHNode<R> nd = nodes[cur];
+            const R xd = me.x - nd.c.x, yd = me.y - nd.c.y;
+            const R d2 = xd * xd + yd * yd;
+            if (d2 * theta2 > nd.c.w) {
+                cur = nd.t.y;
+            } else if (nd.t.w - nd.t.z >= 8) {
+                cur = nd.t.x;
+            } else {
+                pairs += nd.t.w - nd.t.z + 1 - (k >= nd.t.z && k <= nd.t.w);
+                cur = nd.t.y;
+            }
+        }
+    }
+    visits = warp_sum(visits);
+    pairs = warp_sum(pairs);
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(counts, visits);
+        atomicAdd(counts + 1, pairs);
+    }
+}
+
+// ---- 6. gravity and attraction (pipeline.cl:389-429) -----------------------
+
+template <class R>
+__global__ void __launch_bounds__(256)
+k_attract(int n, R gravity, int strong, int linlog, int adjust,
+          const typename RT<R>::R2 *__restrict__ pos, const R *__restrict__ mass,
+          const R *__restrict__ size, const int *__restrict__ off,
+          const Inc<R> *__restrict__ inc, typename RT<R>::R2 *__restrict__ f)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const typename RT<R>::R2 p = pos[i];
+    const R xi = p.x, yi = p.y;
+    typename RT<R>::R2 a = f[i];
+    R ax = a.x, ay = a.y;
+    if (gravity != R(0)) {
+        const R dist = fsqrt(xi * xi + yi * yi);
+        if (dist > R(0)) {
+            const R g = strong ? gravity * mass[i] : fdiv(gravity * mass[i], dist);
+            ax -= xi * g;
+            ay -= yi * g;
+        }
+    }
+    const R si = adjust ? size[i] : R(0);
+    const int e1 = off[i + 1];
+    for (int e = off[i]; e < e1; e++) {
+        const Inc<R> c = inc[e];
+        const typename RT<R>::R2 q = pos[c.j];
+        const R xd = xi - q.x, yd = yi - q.y;
+        R g = -c.coef;
+        if (adjust || linlog) {
+            R dist = fsqrt(xd * xd + yd * yd);
+            if (adjust) dist -= si + size[c.j];
+            if (!(dist > R(0))) continue;
+            if (linlog) g *= fdiv(flog1p(dist), dist);
+        }
+        ax += xd * g;
+        ay += yd * g;
+    }
+    f[i] = mk2<R>(ax, ay);
+}
+
+// ---- 7. swinging, traction, FP64 totals and the speed update --------------
+// Per node: swing in the device precision (kept for the displacement); the
+// totals over the nodes that can move are summed in double: per thread over a
+// fixed set of nodes, per block in a fixed tree order, then by the last block
+// over the block partials with Neumaier compensation. The same block then
+// updates Gephi's adaptive speed in double (reference
+// src/forceatlas2.c:443-485), so no total ever goes to the host.
+
+__device__ __forceinline__ void neumaier(double &s, double &c, double v)
+{
+    const double t = __dadd_rn(s, v);
+    if (fabs(s) >= fabs(v))
+        c = __dadd_rn(c, __dadd_rn(__dsub_rn(s, t), v));
+    else
+        c = __dadd_rn(c, __dadd_rn(__dsub_rn(v, t), s));
+    s = t;
+}
+
+__device__ inline void update_speed_dev(SpeedState *st, double tsw, double ttr)
+{
+    double speed = st->speed, eff = st->efficiency;
+    st->total_swinging = tsw;
+    st->total_traction = ttr;
+    if (!(tsw > 0)) return;
+    const int n = st->n;
+    const double jitter = st->jitter_tolerance;
+    const double est = __dmul_rn(0.05, sqrt((double) n));
+    const double min_jt = sqrt(est), max_jt = 10.0;
+    double jt = __ddiv_rn(__dmul_rn(est, ttr), __dmul_rn((double) n, (double) n));
+    if (jt > max_jt) jt = max_jt;
+    if (jt < min_jt) jt = min_jt;
+    jt = __dmul_rn(jt, jitter);
+    if (tsw > __dmul_rn(2.0, ttr)) {
+        if (eff > 0.05) eff = __dmul_rn(eff, 0.5);
+        if (jt < jitter) jt = jitter;
+    }
+    const double target = __ddiv_rn(__dmul_rn(__dmul_rn(jt, eff), ttr), tsw);
+    if (tsw > __dmul_rn(jt, ttr)) {
+        if (eff > 0.05) eff = __dmul_rn(eff, 0.7);
+    } else if (speed < 1000) {
+        eff = __dmul_rn(eff, 1.3);
+    }
+    const double rise = __dsub_rn(target, speed);
+    const double cap = __dmul_rn(0.5, speed);
+    speed = __dadd_rn(speed, rise < cap ? rise : cap);
+    st->speed = speed;
+    st->efficiency = eff;
+}
+
+template <class R>
+__global__ void __launch_bounds__(256)
+k_swing(int n, const typename RT<R>::R2 *__restrict__ f,
+        const typename RT<R>::R2 *__restrict__ fold, const R *__restrict__ mass,
+        const uint8_t *__restrict__ fixed, R *__restrict__ sw,
+        double2 *__restrict__ partial, unsigned *__restrict__ ticket,
+        SpeedState *__restrict__ st, int *__restrict__ status)
+{
+    double as = 0.0, at = 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += gridDim.x * blockDim.x) {
+        const typename RT<R>::R2 a = f[i], b = fold[i];
+        const R sx = b.x - a.x, sy = b.y - a.y;
+        const R tx = b.x + a.x, ty = b.y + a.y;
+        const R m = mass[i];
+        const R s = m * fsqrt(sx * sx + sy * sy);
+        sw[i] = s;
+        if (fixed && fixed[i]) continue;
+        as = __dadd_rn(as, (double) s);
+        at = __dadd_rn(at, (double) (R(0.5) * m * fsqrt(tx * tx + ty * ty)));
+    }
+    as = warp_sum(as);
+    at = warp_sum(at);
+    __shared__ double ss[8], st_[8];
+    __shared__ int last;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (lane == 0) {
+        ss[w] = as;
+        st_[w] = at;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double a = 0.0, b = 0.0;
+        for (int k = 0; k < (int) (blockDim.x >> 5); k++) {
+            a = __dadd_rn(a, ss[k]);
+            b = __dadd_rn(b, st_[k]);
+        }
+        partial[blockIdx.x] = make_double2(a, b);
+        __threadfence();
+        last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    double s1 = 0.0, c1 = 0.0, s2 = 0.0, c2 = 0.0;
+    for (int k = threadIdx.x; k < (int) gridDim.x; k += blockDim.x) {
+        const double2 v = __ldcg(partial + k);
+        neumaier(s1, c1, v.x);
+        neumaier(s2, c2, v.y);
+    }
+    __shared__ double r1[256], r2[256];
+    r1[threadIdx.x] = __dadd_rn(s1, c1);
+    r2[threadIdx.x] = __dadd_rn(s2, c2);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t1 = 0.0, k1 = 0.0, t2 = 0.0, k2 = 0.0;
+        for (int k = 0; k < (int) blockDim.x; k++) {
+            neumaier(t1, k1, r1[k]);
+            neumaier(t2, k2, r2[k]);
+        }
+        const double tsw = __dadd_rn(t1, k1), ttr = __dadd_rn(t2, k2);
+        *ticket = 0u;
+        if (!(tsw == tsw) || !(ttr == ttr)) {
+            atomicOr(status + ST_ERROR, ERR_NAN);
+            st->total_swinging = tsw;
+            st->total_traction = ttr;
+        } else {
+            update_speed_dev(st, tsw, ttr);
+        }
+    }
+}
+
+// ---- 8. displacement (pipeline.cl:476-506) ---------------------------------
+
+template <class R>
+__global__ void __launch_bounds__(256)
+k_apply(int n, int adjust, const typename RT<R>::R2 *__restrict__ f,
+        typename RT<R>::R2 *__restrict__ fold, const R *__restrict__ sw,
+        const uint8_t *__restrict__ fixed, typename RT<R>::R2 *__restrict__ pos,
+        const SpeedState *__restrict__ st, const int *__restrict__ status)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    if (status[ST_ERROR]) return; // the layout stopped: keep every position
+    const R speed = (R) st->speed;
+    const typename RT<R>::R2 a = f[i];
+    fold[i] = a;
+    if (fixed && fixed[i]) return;
+    R factor;
+    if (adjust) {
+        const R df = fsqrt(a.x * a.x + a.y * a.y);
+        factor = fdiv(R(0.1) * speed, R(1) + fsqrt(speed * sw[i]));
+        if (df > R(0)) {
+            if (factor * df > R(10)) factor = fdiv(R(10), df);
+        } else {
+            factor = R(0);
+        }
+    } else {
+        factor = fdiv(speed, R(1) + fsqrt(speed * sw[i]));
+    }
+    typename RT<R>::R2 p = pos[i];
+    p.x += a.x * factor;
+    p.y += a.y * factor;
+    pos[i] = p;
+}
+
+// ---- conversions between the host's doubles and the device layout --------
+
+template <class R>
+__global__ void __launch_bounds__(256)
+k_pos_in(int n, const double *__restrict__ xy, typename RT<R>::R2 *__restrict__ pos)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) pos[i] = mk2<R>((R) xy[i], (R) xy[n + i]);
+}
+
+template <class R>
+__global__ void __launch_bounds__(256)
+k_pos_out(int n, const typename RT<R>::R2 *__restrict__ pos, double *__restrict__ xy)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const typename RT<R>::R2 p = pos[i];
+    xy[i] = (double) p.x;
+    xy[n + i] = (double) p.y;
+}
+
+template <class R>
+__global__ void __launch_bounds__(256)
+k_real_in(int n, const double *__restrict__ in, R *__restrict__ out)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = (R) in[i];
+}
+
+template <class R>
+__global__ void __launch_bounds__(256)
+k_inc_in(int ninc, const int *__restrict__ node, const double *__restrict__ coef,
+         Inc<R> *__restrict__ inc)
+{
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= ninc) return;
+    Inc<R> c;
+    c.j = node[e];
+    c.coef = (R) coef[e];
+    inc[e] = c;
+}
+
+// (x, y, m, r) records of every node in original order (the exact kernel's
+// input); r = 0 unless adjust.
+template <class R>
+__global__ void __launch_bounds__(256)
+k_pack(int n, int adjust, const typename RT<R>::R2 *__restrict__ pos,
+       const R *__restrict__ mass, const R *__restrict__ size,
+       typename RT<R>::R4 *__restrict__ out)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const typename RT<R>::R2 p = pos[i];
+    out[i] = mk4<R>(p.x, p.y, mass[i], adjust ? size[i] : R(0));
+}
+
+// Same records from four host-layout double arrays (fa2_gpu_repulse_*).
+template <class R>
+__global__ void __launch_bounds__(256)
+k_pack_host(int n, const double *__restrict__ x, const double *__restrict__ y,
+            const double *__restrict__ m, const double *__restrict__ s,
+            typename RT<R>::R4 *__restrict__ out)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    out[i] = mk4<R>((R) x[i], (R) y[i], (R) m[i], s ? (R) s[i] : R(0));
+}
+
+// Forces to two double arrays, through a permutation when perm != NULL
+// (reference src/gpu.c:520-533).
+template <class R>
+__global__ void __launch_bounds__(256)
+k_forces_out(int n, const typename RT<R>::R2 *__restrict__ f, const int *__restrict__ perm,
+             double *__restrict__ fx, double *__restrict__ fy)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const int i = perm ? perm[k] : k;
+    const typename RT<R>::R2 v = f[k];
+    fx[i] = (double) v.x;
+    fy[i] = (double) v.y;
+}
+
+// ---- exact repulsion: the n-body tile kernel ------------------------------
+// Each thread owns IPT nodes (i, i + T, ...) and sums over every j in
+// ascending order, as the reference (src/forceatlas2.c:278-294). Tiles of
+// (x, y, m, r) records are staged in shared memory by TMA bulk copies
+// (cp.async.bulk, completion on an mbarrier), two tiles in flight. The pair
+// i == j contributes exactly zero (xd = yd = 0 with a finite factor), so no
+// test is needed. Every mbarrier wait is bounded in time: on expiry the
+// kernel records ERR_WAIT, drains its copies in flight and returns.
+
+#define FA2_EXACT_THREADS 128
+
+__device__ __forceinline__ uint32_t smem_addr(const void *p)
+{
+    return (uint32_t) __cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ unsigned long long global_ns()
+{
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, unsigned count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count)
+                 : "memory");
+}
+
+// Bulk copy of `bytes` (a multiple of 16, both addresses 16-byte aligned)
+// from global to shared memory, completing on `bar`.
+__device__ __forceinline__ void tma_load_1d(void *dst, const void *src, unsigned bytes,
+                                            uint64_t *bar)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)),
+                 "r"(bytes)
+                 : "memory");
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_addr(dst)),
+        "l"(src), "r"(bytes), "r"(smem_addr(bar))
+        : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try(uint64_t *bar, unsigned phase)
+{
+    unsigned ok;
+    asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+                 " selp.u32 %0, 1, 0, p;\n}"
+                 : "=r"(ok)
+                 : "r"(smem_addr(bar)), "r"(phase)
+                 : "memory");
+    return ok != 0;
+}
+
+// Wait for a phase of `bar`, for at most `limit_ns` nanoseconds.
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, unsigned phase,
+                                          unsigned long long limit_ns)
+{
+    if (mbar_try(bar, phase)) return true;
+    const unsigned long long t0 = global_ns();
+    for (;;) {
+        if (mbar_try(bar, phase)) return true;
+        if (global_ns() - t0 > limit_ns) return false;
+    }
+}
+
+template <class R, bool ADJUST, int IPT>
+__global__ void __launch_bounds__(FA2_EXACT_THREADS)
+k_exact(int n, R scaling, const typename RT<R>::R4 *__restrict__ nodes,
+        typename RT<R>::R2 *__restrict__ f, int *__restrict__ status)
+{
+    typedef typename RT<R>::R4 R4;
+    constexpr int TILE = 32768 / sizeof(R4); // records per 32 KB tile
+    extern __shared__ __align__(128) unsigned char smem[];
+    R4 *tile = reinterpret_cast<R4 *>(smem);
+    uint64_t *bar = reinterpret_cast<uint64_t *>(smem + 2 * TILE * sizeof(R4));
+    __shared__ int failed;
+
+    R xi[IPT], yi[IPT], mi[IPT], si[IPT], ax[IPT], ay[IPT];
+    const int i0 = blockIdx.x * (FA2_EXACT_THREADS * IPT) + threadIdx.x;
+#pragma unroll
+    for (int u = 0; u < IPT; u++) {
+        const int i = i0 + u * FA2_EXACT_THREADS;
+        const R4 p = nodes[i < n ? i : n - 1];
+        xi[u] = p.x;
+        yi[u] = p.y;
+        mi[u] = p.z;
+        si[u] = p.w;
+        ax[u] = ay[u] = R(0);
+    }
+    const int ntiles = (n + TILE - 1) / TILE;
+    if (threadIdx.x == 0) {
+        failed = 0;
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int t = 0; t < 2 && t < ntiles; t++) {
+            const int cnt = min(TILE, n - t * TILE);
+            tma_load_1d(tile + t * TILE, nodes + (size_t) t * TILE, cnt * (unsigned) sizeof(R4),
+                        &bar[t]);
+        }
+    }
+    for (int t = 0; t < ntiles; t++) {
+        const int b = t & 1;
+        if (!mbar_wait(&bar[b], (t >> 1) & 1, 2000000000ull)) failed = 1;
+        __syncthreads();
+        if (failed) {
+            // drain what may still be in flight, then give up
+            if (threadIdx.x == 0) {
+                atomicOr(status + ST_ERROR, ERR_WAIT);
+                for (int u = t; u < t + 2 && u < ntiles; u++)
+                    mbar_wait(&bar[u & 1], (u >> 1) & 1, 2000000000ull);
+            }
+            __syncthreads();
+            return;
+        }
+        const R4 *q = tile + b * TILE;
+        const int cnt = min(TILE, n - t * TILE);
+#pragma unroll 4
+        for (int jj = 0; jj < cnt; jj++) {
+            const R4 p = q[jj];
+#pragma unroll
+            for (int u = 0; u < IPT; u++) {
+                const R xd = xi[u] - p.x, yd = yi[u] - p.y;
+                const R g = rep_factor<R, ADJUST>(xd * xd + yd * yd, mi[u] * p.z,
+                                                  si[u] + p.w, scaling);
+                ax[u] += xd * g;
+                ay[u] += yd * g;
+            }
+        }
+        __syncthreads(); // every thread is done with buffer b
+        if (threadIdx.x == 0 && t + 2 < ntiles) {
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            const int cnt2 = min(TILE, n - (t + 2) * TILE);
+            tma_load_1d(tile + b * TILE, nodes + (size_t) (t + 2) * TILE,
+                        cnt2 * (unsigned) sizeof(R4), &bar[b]);
+        }
+    }
+#pragma unroll
+    for (int u = 0; u < IPT; u++) {
+        const int i = i0 + u * FA2_EXACT_THREADS;
+        if (i < n) f[i] = mk2<R>(ax[u], ay[u]);
+    }
+}
+
+template <class R> constexpr size_t exact_smem_bytes()
+{
+    return 2 * 32768 + 2 * sizeof(uint64_t);
+}
+
+// ---- quadtree traversal of fa2_gpu_repulse_bh (reference src/gpu.c:78-123)
+// Regions of the host's Gephi quadtree, converted on the device.
+
+template <class R>
+__global__ void __launch_bounds__(256)
+k_qregions(int nreg, const fa2_region *__restrict__ reg, QRegion<R> *__restrict__ out)
+{
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= nreg) return;
+    const fa2_region g = reg[r];
+    QRegion<R> q;
+    q.rr = mk4<R>((R) g.cx, (R) g.cy, (R) g.mass, (R) (g.size * g.size));
+    q.ri = make_int4(g.start, g.count, g.nchild > 0 ? g.child + g.nchild - 1 : -1, g.skip);
+    out[r] = q;
+}
+
+// Stackless walk over the quadtree: go down to the last child or jump to
+// `skip` (the previous sibling, else the parent's skip), the visiting order of
+// the CPU's stack (src/forceatlas2.c:326-368). Nodes in tree order; the
+// output is in tree order too.
+template <class R, bool ADJUST>
+__global__ void __launch_bounds__(256)
+k_qtraverse(int n, R scaling, R theta2, const typename RT<R>::R4 *__restrict__ p,
+            const QRegion<R> *__restrict__ reg, int nreg,
+            typename RT<R>::R2 *__restrict__ f, int *__restrict__ status)
+{
+    typedef typename RT<R>::R4 R4;
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const R4 me = p[k];
+    const R xi = me.x, yi = me.y, mi = me.z, si = me.w;
+    R ax = R(0), ay = R(0);
+    int cur = 0, j = 0, jend = -1;
+    const int cap = 2 * nreg + 2 * n + 64;
+    for (int step = 0;; step++) {
+        if (step > cap || cur >= nreg || jend >= n) {
+            atomicOr(status + ST_ERROR, ERR_BOUNDS);
+            break;
+        }
+        if (j <= jend) {
+            if (j != k) {
+                const R4 q = p[j];
+                const R xd = xi - q.x, yd = yi - q.y;
+                const R g = rep_factor<R, ADJUST>(xd * xd + yd * yd, mi * q.z,
+                                                  si + q.w, scaling);
+                ax += xd * g;
+                ay += yd * g;
+            }
+            ++j;
+            continue;
+        }
+        if (cur < 0) break;
+        const QRegion<R> q = reg[cur];
+        if (q.ri.y > 1) {
+            const R xd = xi - q.rr.x, yd = yi - q.rr.y;
+            const R d2 = xd * xd + yd * yd;
+            if (d2 * theta2 > q.rr.w) {
+                const R g = fdiv(scaling * (mi * q.rr.z), d2);
+                ax += xd * g;
+                ay += yd * g;
+                cur = q.ri.w;
+                continue;
+            }
+            if (q.ri.z >= 0) {
+                cur = q.ri.z;
+                continue;
+            }
+        }
+        j = q.ri.x;
+        jend = q.ri.x + q.ri.y - 1;
+        cur = q.ri.w;
+    }
+    f[k] = mk2<R>(ax, ay);
+}
+
+} // namespace fa2cu

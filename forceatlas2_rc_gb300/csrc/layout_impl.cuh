@@ -1,0 +1,680 @@
+// layout_impl.cuh -- the device sessions, templated on the real type.
+// Included by inst_f32.cu and inst_f64.cu only, so that every kernel they
+// launch is compiled with the flags of its precision.
+//
+// HBM layout of a Layout<R> (n nodes, E incidences; float sizes):
+//   pos, f, fold        R2[n]   positions, forces, previous forces
+//   mass, size, sw      R[n]    masses, radii (adjust), swinging
+//   fixed               u8[n]   (when some node is fixed)
+//   inc_off, inc        int[n+1], {int j; R coef}[E]  symmetric CSR
+//   key, order (+ ping-pong)  u32[n] x 4, counts u32[256 * n / 4096]
+//   psort               R4[n]   (x, y, m, r) in Morton order
+//   child, range        int2[n-1], parent int[2n-1], rope int[n],
+//   visits              int[n-1], agg Agg<R>[n-1], nodes BHNode<R>[n-1]
+//   packed              R4[n]   (exact repulsion only)
+//   st, status          FP64 speed state, status words
+#pragma once
+
+#include <stdio.h>
+#include <string.h>
+#include <time.h>
+#include <vector>
+
+#include "kernels.cuh"
+#include "session.h"
+#include "sort_tree.cuh"
+
+namespace fa2cu {
+
+inline double now_s()
+{
+    struct timespec ts;
+    clock_gettime(CLOCK_MONOTONIC, &ts);
+    return (double) ts.tv_sec + 1e-9 * (double) ts.tv_nsec;
+}
+
+// Device allocations of a session, released together.
+struct DevMem {
+    std::vector<void *> ptrs;
+    double bytes = 0.0;
+    bool failed = false;
+    cudaError_t err = cudaSuccess;
+    template <class T> T *get(size_t count)
+    {
+        if (failed) return nullptr;
+        void *p = nullptr;
+        const size_t b = (count > 0 ? count : 1) * sizeof(T);
+        err = cudaMalloc(&p, b);
+        if (err != cudaSuccess) {
+            failed = true;
+            return nullptr;
+        }
+        ptrs.push_back(p);
+        bytes += (double) b;
+        return (T *) p;
+    }
+    void release()
+    {
+        for (void *p : ptrs) cudaFree(p);
+        ptrs.clear();
+    }
+};
+
+template <class R> struct Layout : LayoutBase {
+    typedef typename RT<R>::R2 R2;
+    typedef typename RT<R>::R4 R4;
+
+    int n = 0, ninc = 0, repulsion = 0, adjust = 0, strong = 0, linlog = 0;
+    int any_fixed = 0;
+    R scaling = 0, gravity = 0, theta2 = 0;
+    cudaStream_t s = nullptr;
+    DevMem mem;
+    R2 *pos = nullptr, *f = nullptr, *fold = nullptr;
+    R *mass = nullptr, *size = nullptr, *sw = nullptr;
+    uint8_t *fixed = nullptr;
+    int *inc_off = nullptr;
+    Inc<R> *inc = nullptr;
+    R *bbox = nullptr, *bbox_partial = nullptr;
+    int nbbox = 1, nswing = 1;
+    uint32_t *key = nullptr, *order = nullptr;
+    SortScratch ss{};
+    R4 *psort = nullptr, *packed = nullptr;
+    int2 *child = nullptr, *range = nullptr;
+    int *parent = nullptr, *rope = nullptr, *visits = nullptr;
+    Agg<R> *agg = nullptr;
+    BHNode<R> *nodes = nullptr;
+    double2 *swing_partial = nullptr;
+    SpeedState *st = nullptr;
+    int *status = nullptr;
+    double *xy = nullptr; // 2n doubles of staging
+    unsigned long long *counts = nullptr;
+    cudaGraphExec_t g1 = nullptr, g8 = nullptr;
+    cudaEvent_t ev[8] = {};
+
+    ~Layout() override
+    {
+        if (s) cudaStreamSynchronize(s);
+        if (g1) cudaGraphExecDestroy(g1);
+        if (g8) cudaGraphExecDestroy(g8);
+        for (auto &e : ev)
+            if (e) cudaEventDestroy(e);
+        mem.release();
+        if (s) cudaStreamDestroy(s);
+    }
+
+    double bytes() const override { return mem.bytes; }
+    cudaStream_t stream() override { return s; }
+
+    int alloc(bool want_tree)
+    {
+        const size_t nn = (size_t) n;
+        pos = mem.get<R2>(nn);
+        f = mem.get<R2>(nn);
+        fold = mem.get<R2>(nn);
+        mass = mem.get<R>(nn);
+        size = adjust ? mem.get<R>(nn) : nullptr;
+        sw = mem.get<R>(nn);
+        fixed = any_fixed ? mem.get<uint8_t>(nn) : nullptr;
+        inc_off = mem.get<int>(nn + 1);
+        inc = mem.get<Inc<R>>((size_t) ninc);
+        nswing = std::min(ceil_div(n, 256), 152 * 8);
+        swing_partial = mem.get<double2>((size_t) nswing);
+        st = mem.get<SpeedState>(1);
+        status = mem.get<int>(ST_COUNT);
+        xy = mem.get<double>(2 * nn);
+        counts = mem.get<unsigned long long>(2);
+        if (want_tree) {
+            nbbox = std::min(ceil_div(n, 256), 152 * 4);
+            bbox = mem.get<R>(4);
+            bbox_partial = mem.get<R>(4 * (size_t) nbbox);
+            key = mem.get<uint32_t>(nn);
+            order = mem.get<uint32_t>(nn);
+            ss.key_b = mem.get<uint32_t>(nn);
+            ss.val_b = mem.get<uint32_t>(nn);
+            ss.counts = mem.get<uint32_t>(sort_scratch_counts(n));
+            ss.digit_total = mem.get<uint32_t>(256);
+            psort = mem.get<R4>(nn);
+            child = mem.get<int2>(nn - 1);
+            range = mem.get<int2>(nn - 1);
+            parent = mem.get<int>(2 * nn - 1);
+            rope = mem.get<int>(nn);
+            visits = mem.get<int>(nn - 1);
+            agg = mem.get<Agg<R>>(nn - 1);
+            nodes = mem.get<BHNode<R>>(nn - 1);
+        } else {
+            packed = mem.get<R4>(nn);
+        }
+        if (mem.failed) {
+            set_cuda_error("could not allocate memory on the device", mem.err);
+            return 1;
+        }
+        return 0;
+    }
+
+    int open(const fa2_full_params *p, const double *xy0, int rep)
+    {
+        n = p->n;
+        ninc = p->inc_off[n];
+        repulsion = rep;
+        adjust = p->adjust ? 1 : 0;
+        strong = p->strong ? 1 : 0;
+        linlog = p->linlog ? 1 : 0;
+        any_fixed = 0;
+        if (p->fixed)
+            for (int i = 0; i < n && !any_fixed; i++) any_fixed = p->fixed[i] != 0;
+        scaling = (R) p->scaling;
+        gravity = (R) p->gravity;
+        theta2 = (R) (p->theta * p->theta);
+        FA2_TRY(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking),
+                "could not create a CUDA stream", 1);
+        for (auto &e : ev) FA2_TRY(cudaEventCreate(&e), "could not create a CUDA event", 1);
+        if (alloc(rep == FA2CU_REPULSION_BH)) return 1;
+
+        // the graph, once (reference src/gpu_full.c:241-287)
+        {
+            DevMem tmp;
+            double *dd = tmp.get<double>(std::max<size_t>((size_t) n, (size_t) ninc));
+            int *di = tmp.get<int>((size_t) ninc);
+            if (tmp.failed) {
+                tmp.release();
+                set_cuda_error("could not allocate memory on the device", tmp.err);
+                return 1;
+            }
+            int rc = 0;
+            auto up = [&](void *dst, const void *src, size_t b) {
+                if (!rc && b) rc = cudaMemcpyAsync(dst, src, b, cudaMemcpyHostToDevice, s) != cudaSuccess;
+            };
+            up(dd, p->mass, (size_t) n * sizeof(double));
+            if (!rc) k_real_in<R><<<ceil_div(n, 256), 256, 0, s>>>(n, dd, mass);
+            if (adjust) {
+                up(dd, p->size, (size_t) n * sizeof(double));
+                if (!rc) k_real_in<R><<<ceil_div(n, 256), 256, 0, s>>>(n, dd, size);
+            }
+            up(inc_off, p->inc_off, ((size_t) n + 1) * sizeof(int));
+            if (ninc > 0) {
+                up(dd, p->inc_coef, (size_t) ninc * sizeof(double));
+                up(di, p->inc_node, (size_t) ninc * sizeof(int));
+                if (!rc) k_inc_in<R><<<ceil_div(ninc, 256), 256, 0, s>>>(ninc, di, dd, inc);
+            }
+            if (any_fixed) {
+                std::vector<uint8_t> f8((size_t) n);
+                for (int i = 0; i < n; i++) f8[i] = p->fixed[i] != 0;
+                up(fixed, f8.data(), (size_t) n);
+                if (!rc) rc = cudaStreamSynchronize(s) != cudaSuccess;
+            }
+            if (!rc) rc = cudaStreamSynchronize(s) != cudaSuccess;
+            tmp.release();
+            if (rc) {
+                set_cuda_error("could not send the graph to the device", cudaGetLastError());
+                return 1;
+            }
+        }
+        if (set_positions(xy0)) return 1;
+        FA2_TRY(cudaMemsetAsync(fold, 0, (size_t) n * sizeof(R2), s), "cudaMemset", 1);
+        FA2_TRY(cudaMemsetAsync(status, 0, ST_COUNT * sizeof(int), s), "cudaMemset", 1);
+        SpeedState h{};
+        h.speed = 1.0;
+        h.efficiency = 1.0;
+        h.jitter_tolerance = p->jitter_tolerance;
+        h.n = n;
+        FA2_TRY(cudaMemcpyAsync(st, &h, sizeof(h), cudaMemcpyHostToDevice, s), "cudaMemcpy", 1);
+        if (repulsion == FA2CU_REPULSION_EXACT) {
+            const size_t smem = exact_smem_bytes<R>();
+            FA2_TRY(cudaFuncSetAttribute(k_exact<R, false, EXACT_IPT>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem),
+                    "cudaFuncSetAttribute", 1);
+            FA2_TRY(cudaFuncSetAttribute(k_exact<R, true, EXACT_IPT>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem),
+                    "cudaFuncSetAttribute", 1);
+        }
+        FA2_TRY(cudaStreamSynchronize(s), "could not prepare the layout", 1);
+        if (capture(&g1, 1)) return 1;
+        if (n <= (1 << 16) && capture(&g8, 8)) return 1;
+        return 0;
+    }
+
+    static constexpr int EXACT_IPT = sizeof(R) == 4 ? 2 : 1;
+
+    // ---- the steps of one iteration ----
+    void launch_build()
+    {
+        k_bbox<R><<<nbbox, 256, 0, s>>>(n, pos, bbox_partial, bbox,
+                                        (unsigned *) (status + ST_TICKET_BBOX));
+        k_morton<R><<<ceil_div(n, 256), 256, 0, s>>>(n, pos, bbox, key, order);
+    }
+    void launch_sort() { sort_pairs(s, n, key, order, ss); }
+    void launch_tree()
+    {
+        k_gather<R><<<ceil_div(n, 256), 256, 0, s>>>(n, adjust, order, pos, mass, size, psort,
+                                                     status);
+        karras_tree(s, n, key, child, range, parent, rope, visits);
+        k_aggregate<R><<<ceil_div(n, 256), 256, 0, s>>>(n, psort, child, parent, range, rope,
+                                                        visits, agg, nodes, status);
+    }
+    void launch_repulsion()
+    {
+        if (repulsion == FA2CU_REPULSION_BH) {
+            if (adjust)
+                k_traverse<R, true><<<ceil_div(n, 256), 256, 0, s>>>(n, scaling, theta2, psort,
+                                                                     nodes, rope, order, f,
+                                                                     status);
+            else
+                k_traverse<R, false><<<ceil_div(n, 256), 256, 0, s>>>(n, scaling, theta2, psort,
+                                                                      nodes, rope, order, f,
+                                                                      status);
+        } else {
+            k_pack<R><<<ceil_div(n, 256), 256, 0, s>>>(n, adjust, pos, mass, size, packed);
+            const int grid = ceil_div(n, FA2_EXACT_THREADS * EXACT_IPT);
+            const size_t smem = exact_smem_bytes<R>();
+            if (adjust)
+                k_exact<R, true, EXACT_IPT><<<grid, FA2_EXACT_THREADS, smem, s>>>(
+                    n, scaling, packed, f, status);
+            else
+                k_exact<R, false, EXACT_IPT><<<grid, FA2_EXACT_THREADS, smem, s>>>(
+                    n, scaling, packed, f, status);
+        }
+    }
+    void launch_attraction()
+    {
+        k_attract<R><<<ceil_div(n, 256), 256, 0, s>>>(n, gravity, strong, linlog, adjust, pos,
+                                                      mass, size, inc_off, inc, f);
+    }
+    void launch_move()
+    {
+        k_swing<R><<<nswing, 256, 0, s>>>(n, f, fold, mass, fixed, sw, swing_partial,
+                                          (unsigned *) (status + ST_TICKET_SWING), st, status);
+        k_apply<R><<<ceil_div(n, 256), 256, 0, s>>>(n, adjust, f, fold, sw, fixed, pos, st,
+                                                    status);
+    }
+    void launch_forces()
+    {
+        if (repulsion == FA2CU_REPULSION_BH) {
+            launch_build();
+            launch_sort();
+            launch_tree();
+        }
+        launch_repulsion();
+        launch_attraction();
+    }
+    void launch_iteration()
+    {
+        launch_forces();
+        launch_move();
+    }
+
+    int capture(cudaGraphExec_t *out, int iters)
+    {
+        cudaGraph_t g = nullptr;
+        FA2_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal),
+                "could not capture the iteration", 1);
+        for (int k = 0; k < iters; k++) launch_iteration();
+        cudaError_t e = cudaStreamEndCapture(s, &g);
+        if (e != cudaSuccess) {
+            set_cuda_error("could not capture the iteration", e);
+            return 1;
+        }
+        e = cudaGraphInstantiate(out, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) {
+            set_cuda_error("could not instantiate the iteration graph", e);
+            return 1;
+        }
+        return 0;
+    }
+
+    int iterate(int iterations) override
+    {
+        cudaSetDevice(device);
+        while (iterations >= 8 && g8) {
+            FA2_TRY(cudaGraphLaunch(g8, s), "the computation on the GPU failed", 1);
+            iterations -= 8;
+        }
+        for (; iterations > 0; iterations--)
+            FA2_TRY(cudaGraphLaunch(g1, s), "the computation on the GPU failed", 1);
+        return 0;
+    }
+
+    int sync() override
+    {
+        cudaSetDevice(device);
+        FA2_TRY(cudaStreamSynchronize(s), "the computation on the GPU failed", 1);
+        int h = 0;
+        FA2_TRY(cudaMemcpy(&h, status + ST_ERROR, sizeof(int), cudaMemcpyDeviceToHost),
+                "the computation on the GPU failed", 1);
+        if (h & ERR_NAN) {
+            set_message("the computation on the GPU produced invalid numbers");
+            return 1;
+        }
+        if (h & ERR_WAIT) {
+            set_message("the computation on the GPU failed (a device wait timed out)");
+            return 1;
+        }
+        if (h & ERR_BOUNDS) {
+            set_message("the computation on the GPU failed (an index left its bounds)");
+            return 1;
+        }
+        return 0;
+    }
+
+    int positions(double *out) override
+    {
+        cudaSetDevice(device);
+        k_pos_out<R><<<ceil_div(n, 256), 256, 0, s>>>(n, pos, xy);
+        FA2_TRY(cudaMemcpyAsync(out, xy, 2 * (size_t) n * sizeof(double),
+                                cudaMemcpyDeviceToHost, s),
+                "could not fetch the layout from the device", 1);
+        FA2_TRY(cudaStreamSynchronize(s), "could not fetch the layout from the device", 1);
+        return 0;
+    }
+
+    int set_positions(const double *in) override
+    {
+        cudaSetDevice(device);
+        FA2_TRY(cudaMemcpyAsync(xy, in, 2 * (size_t) n * sizeof(double),
+                                cudaMemcpyHostToDevice, s),
+                "could not send the positions to the device", 1);
+        k_pos_in<R><<<ceil_div(n, 256), 256, 0, s>>>(n, xy, pos);
+        FA2_TRY(cudaStreamSynchronize(s), "could not send the positions to the device", 1);
+        return 0;
+    }
+
+    int forces(const double *in, double *out) override
+    {
+        if (set_positions(in)) return 1;
+        launch_forces();
+        k_forces_out<R><<<ceil_div(n, 256), 256, 0, s>>>(n, f, nullptr, xy, xy + n);
+        FA2_TRY(cudaMemcpyAsync(out, xy, 2 * (size_t) n * sizeof(double),
+                                cudaMemcpyDeviceToHost, s),
+                "could not fetch the forces", 1);
+        return sync();
+    }
+
+    int speed(double state[4]) override
+    {
+        cudaSetDevice(device);
+        SpeedState h;
+        FA2_TRY(cudaMemcpyAsync(&h, st, sizeof(h), cudaMemcpyDeviceToHost, s), "cudaMemcpy", 1);
+        FA2_TRY(cudaStreamSynchronize(s), "cudaMemcpy", 1);
+        state[0] = h.speed;
+        state[1] = h.efficiency;
+        state[2] = h.total_swinging;
+        state[3] = h.total_traction;
+        return 0;
+    }
+
+    int phase_times(int iterations, double *ms) override
+    {
+        cudaSetDevice(device);
+        for (int it = 0; it < iterations; it++) {
+            int e = 0;
+            cudaEventRecord(ev[e++], s);
+            if (repulsion == FA2CU_REPULSION_BH) {
+                launch_build();
+                cudaEventRecord(ev[e++], s);
+                launch_sort();
+                cudaEventRecord(ev[e++], s);
+                launch_tree();
+                cudaEventRecord(ev[e++], s);
+            } else {
+                cudaEventRecord(ev[e++], s);
+                cudaEventRecord(ev[e++], s);
+                cudaEventRecord(ev[e++], s);
+            }
+            launch_repulsion();
+            cudaEventRecord(ev[e++], s);
+            launch_attraction();
+            cudaEventRecord(ev[e++], s);
+            launch_move();
+            cudaEventRecord(ev[e++], s);
+            FA2_TRY(cudaEventSynchronize(ev[e - 1]), "the computation on the GPU failed", 1);
+            double total = 0.0;
+            for (int k = 1; k < e; k++) {
+                float t = 0.f;
+                cudaEventElapsedTime(&t, ev[k - 1], ev[k]);
+                ms[k] += t;
+                total += t;
+            }
+            ms[FA2_FULL_T_TOTAL] += total;
+        }
+        return sync();
+    }
+
+    int tree(const double *in, uint32_t *hkey, uint32_t *horder, int *hchild, int *hrange,
+             int *hparent, double *hni) override
+    {
+        if (repulsion != FA2CU_REPULSION_BH) {
+            set_message("this layout has no tree (exact repulsion)");
+            return 1;
+        }
+        if (set_positions(in)) return 1;
+        launch_build();
+        launch_sort();
+        launch_tree();
+        std::vector<BHNode<R>> hn((size_t) n - 1);
+        const size_t nn = (size_t) n;
+        cudaMemcpyAsync(hkey, key, nn * 4, cudaMemcpyDeviceToHost, s);
+        cudaMemcpyAsync(horder, order, nn * 4, cudaMemcpyDeviceToHost, s);
+        cudaMemcpyAsync(hchild, child, (nn - 1) * sizeof(int2), cudaMemcpyDeviceToHost, s);
+        cudaMemcpyAsync(hrange, range, (nn - 1) * sizeof(int2), cudaMemcpyDeviceToHost, s);
+        cudaMemcpyAsync(hparent, parent, (2 * nn - 1) * sizeof(int), cudaMemcpyDeviceToHost, s);
+        cudaMemcpyAsync(hn.data(), nodes, (nn - 1) * sizeof(BHNode<R>), cudaMemcpyDeviceToHost, s);
+        FA2_TRY(cudaStreamSynchronize(s), "could not fetch the tree", 1);
+        for (size_t r = 0; r + 1 < nn; r++) {
+            hni[4 * r] = (double) hn[r].c.x;
+            hni[4 * r + 1] = (double) hn[r].c.y;
+            hni[4 * r + 2] = (double) hn[r].c.z;
+            hni[4 * r + 3] = (double) hn[r].c.w;
+        }
+        return 0;
+    }
+
+    int traversal_counts(double out[2]) override
+    {
+        if (repulsion != FA2CU_REPULSION_BH) {
+            set_message("this layout has no tree (exact repulsion)");
+            return 1;
+        }
+        cudaSetDevice(device);
+        launch_build();
+        launch_sort();
+        launch_tree();
+        cudaMemsetAsync(counts, 0, 2 * sizeof(unsigned long long), s);
+        k_traverse_count<R><<<ceil_div(n, 256), 256, 0, s>>>(n, theta2, psort, nodes, rope,
+                                                             counts);
+        unsigned long long h[2] = {0, 0};
+        cudaMemcpyAsync(h, counts, sizeof(h), cudaMemcpyDeviceToHost, s);
+        FA2_TRY(cudaStreamSynchronize(s), "the computation on the GPU failed", 1);
+        out[0] = (double) h[0];
+        out[1] = (double) h[1];
+        return 0;
+    }
+};
+
+template <class R> LayoutBase *make_layout(const fa2_full_params *p, const double *pos, int rep)
+{
+    int dev = p->device;
+    FA2_TRY(cudaSetDevice(dev), "could not use the CUDA device", nullptr);
+    Layout<R> *L = new Layout<R>();
+    L->device = dev;
+    if (L->open(p, pos, rep)) {
+        delete L;
+        return nullptr;
+    }
+    return L;
+}
+
+// ---- the repulsion backend of fa2_gpu_open (reference src/gpu.c:357-704) --
+
+template <class R> struct Repulse : RepulseBase {
+    typedef typename RT<R>::R2 R2;
+    typedef typename RT<R>::R4 R4;
+    int n = 0, adjust = 0, barnes_hut = 0;
+    cudaStream_t s = nullptr;
+    DevMem mem;
+    double *in4 = nullptr;   // x, y, mass, size staging (4n)
+    double *out2 = nullptr;  // fx, fy (2n)
+    double *host2 = nullptr; // pinned copy of out2
+    R4 *p = nullptr;
+    R2 *f = nullptr;
+    int *status = nullptr;
+    fa2_region *raw = nullptr;
+    QRegion<R> *regs = nullptr;
+    int *perm = nullptr;
+
+    ~Repulse() override
+    {
+        if (s) cudaStreamSynchronize(s);
+        mem.release();
+        if (host2) cudaFreeHost(host2);
+        if (s) cudaStreamDestroy(s);
+    }
+
+    int open(int n_, int adjust_, int bh)
+    {
+        n = n_;
+        adjust = adjust_ ? 1 : 0;
+        barnes_hut = bh ? 1 : 0;
+        const size_t nn = (size_t) n;
+        FA2_TRY(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking),
+                "could not create a CUDA stream", 1);
+        in4 = mem.get<double>(4 * nn);
+        out2 = mem.get<double>(2 * nn);
+        p = mem.get<R4>(nn);
+        f = mem.get<R2>(nn);
+        status = mem.get<int>(ST_COUNT);
+        if (barnes_hut) {
+            raw = mem.get<fa2_region>(2 * nn);
+            regs = mem.get<QRegion<R>>(2 * nn);
+            perm = mem.get<int>(nn);
+        }
+        if (mem.failed) {
+            set_cuda_error("could not allocate memory on the device", mem.err);
+            return 1;
+        }
+        FA2_TRY(cudaMallocHost(&host2, 2 * nn * sizeof(double)), "out of memory", 1);
+        FA2_TRY(cudaMemsetAsync(status, 0, ST_COUNT * sizeof(int), s), "cudaMemset", 1);
+        if (!barnes_hut) {
+            const size_t smem = exact_smem_bytes<R>();
+            FA2_TRY(cudaFuncSetAttribute(k_exact<R, false, Layout<R>::EXACT_IPT>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem),
+                    "cudaFuncSetAttribute", 1);
+            FA2_TRY(cudaFuncSetAttribute(k_exact<R, true, Layout<R>::EXACT_IPT>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem),
+                    "cudaFuncSetAttribute", 1);
+        }
+        FA2_TRY(cudaStreamSynchronize(s), "could not prepare the device", 1);
+        return 0;
+    }
+
+    int send4(const double *x, const double *y, const double *m, const double *sz)
+    {
+        const size_t b = (size_t) n * sizeof(double);
+        FA2_TRY(cudaMemcpyAsync(in4, x, b, cudaMemcpyHostToDevice, s), "the computation on the GPU failed", 1);
+        FA2_TRY(cudaMemcpyAsync(in4 + n, y, b, cudaMemcpyHostToDevice, s), "the computation on the GPU failed", 1);
+        FA2_TRY(cudaMemcpyAsync(in4 + 2 * (size_t) n, m, b, cudaMemcpyHostToDevice, s), "the computation on the GPU failed", 1);
+        const bool with_size = adjust && sz;
+        if (with_size)
+            FA2_TRY(cudaMemcpyAsync(in4 + 3 * (size_t) n, sz, b, cudaMemcpyHostToDevice, s),
+                    "the computation on the GPU failed", 1);
+        k_pack_host<R><<<ceil_div(n, 256), 256, 0, s>>>(
+            n, in4, in4 + n, in4 + 2 * (size_t) n, with_size ? in4 + 3 * (size_t) n : nullptr, p);
+        return 0;
+    }
+
+    int fetch_add(const int *dperm, double *dx, double *dy)
+    {
+        double t0 = now_s();
+        k_forces_out<R><<<ceil_div(n, 256), 256, 0, s>>>(n, f, dperm, out2, out2 + n);
+        FA2_TRY(cudaMemcpyAsync(host2, out2, 2 * (size_t) n * sizeof(double),
+                                cudaMemcpyDeviceToHost, s),
+                "the computation on the GPU failed", 1);
+        FA2_TRY(cudaStreamSynchronize(s), "the computation on the GPU failed", 1);
+        for (int i = 0; i < n; i++) {
+            dx[i] += host2[i];
+            dy[i] += host2[n + i];
+        }
+        t_fetch += now_s() - t0;
+        return 0;
+    }
+
+    int check_status()
+    {
+        int h = 0;
+        FA2_TRY(cudaMemcpy(&h, status + ST_ERROR, sizeof(int), cudaMemcpyDeviceToHost),
+                "the computation on the GPU failed", 1);
+        if (h) {
+            set_message(h & ERR_WAIT ? "the computation on the GPU failed (a device wait timed out)"
+                                     : "the computation on the GPU failed (an index left its bounds)");
+            return 1;
+        }
+        return 0;
+    }
+
+    int exact(const double *x, const double *y, const double *m, const double *sz,
+              double sc, double *dx, double *dy) override
+    {
+        cudaSetDevice(device);
+        double t0 = now_s();
+        if (send4(x, y, m, sz)) return 1;
+        FA2_TRY(cudaStreamSynchronize(s), "the computation on the GPU failed", 1);
+        double t1 = now_s();
+        t_send += t1 - t0;
+        const int ipt = Layout<R>::EXACT_IPT;
+        const int grid = ceil_div(n, FA2_EXACT_THREADS * ipt);
+        const size_t smem = exact_smem_bytes<R>();
+        if (adjust)
+            k_exact<R, true, Layout<R>::EXACT_IPT><<<grid, FA2_EXACT_THREADS, smem, s>>>(
+                n, (R) sc, p, f, status);
+        else
+            k_exact<R, false, Layout<R>::EXACT_IPT><<<grid, FA2_EXACT_THREADS, smem, s>>>(
+                n, (R) sc, p, f, status);
+        FA2_TRY(cudaGetLastError(), "the computation on the GPU failed", 1);
+        FA2_TRY(cudaStreamSynchronize(s), "the computation on the GPU failed", 1);
+        if (check_status()) return 1;
+        t_compute += now_s() - t1;
+        return fetch_add(nullptr, dx, dy);
+    }
+
+    int bh(const fa2_tree *t, double sc, double theta, double *dx, double *dy) override
+    {
+        cudaSetDevice(device);
+        if (check_quadtree(n, t)) return 1;
+        double t0 = now_s();
+        if (send4(t->px, t->py, t->pm, t->ps)) return 1;
+        FA2_TRY(cudaMemcpyAsync(raw, t->reg, (size_t) t->nreg * sizeof(fa2_region),
+                                cudaMemcpyHostToDevice, s),
+                "the computation on the GPU failed", 1);
+        FA2_TRY(cudaMemcpyAsync(perm, t->perm, (size_t) n * sizeof(int), cudaMemcpyHostToDevice, s),
+                "the computation on the GPU failed", 1);
+        k_qregions<R><<<ceil_div(t->nreg, 256), 256, 0, s>>>(t->nreg, raw, regs);
+        FA2_TRY(cudaStreamSynchronize(s), "the computation on the GPU failed", 1);
+        double t1 = now_s();
+        t_send += t1 - t0;
+        const R theta2 = (R) (theta * theta);
+        if (adjust)
+            k_qtraverse<R, true><<<ceil_div(n, 256), 256, 0, s>>>(n, (R) sc, theta2, p, regs,
+                                                                  t->nreg, f, status);
+        else
+            k_qtraverse<R, false><<<ceil_div(n, 256), 256, 0, s>>>(n, (R) sc, theta2, p, regs,
+                                                                   t->nreg, f, status);
+        FA2_TRY(cudaGetLastError(), "the computation on the GPU failed", 1);
+        FA2_TRY(cudaStreamSynchronize(s), "the computation on the GPU failed", 1);
+        if (check_status()) return 1;
+        t_compute += now_s() - t1;
+        return fetch_add(perm, dx, dy);
+    }
+};
+
+template <class R> RepulseBase *make_repulse(int device, int n, int adjust, int bh)
+{
+    FA2_TRY(cudaSetDevice(device), "could not use the CUDA device", nullptr);
+    Repulse<R> *g = new Repulse<R>();
+    g->device = device;
+    if (g->open(n, adjust, bh)) {
+        delete g;
+        return nullptr;
+    }
+    return g;
+}
+
+} // namespace fa2cu

@@ -1,0 +1,54 @@
+// session.h -- the two kinds of device session behind the C interface:
+//   Layout   a layout kept on the device between calls (fa2_full_run and
+//            the fa2cu_layout_* entry points);
+//   Repulse  the repulsion backend of fa2_gpu_open / fa2_gpu_repulse_*.
+// Each has a float and a double implementation (inst_f32.cu, inst_f64.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/fa2.h"
+
+namespace fa2cu {
+
+struct LayoutBase {
+    virtual ~LayoutBase() {}
+    virtual int iterate(int iterations) = 0;
+    virtual int sync() = 0;
+    virtual int positions(double *pos) = 0;
+    virtual int set_positions(const double *pos) = 0;
+    virtual int forces(const double *pos, double *f) = 0;
+    virtual int speed(double state[4]) = 0;
+    virtual cudaStream_t stream() = 0;
+    virtual int phase_times(int iterations, double *ms) = 0;
+    virtual int tree(const double *pos, uint32_t *key, uint32_t *order, int *child,
+                     int *range, int *parent, double *ni) = 0;
+    virtual int traversal_counts(double counts[2]) = 0;
+    virtual double bytes() const = 0;
+    int device = 0;
+};
+
+// NULL on failure (message set). `pos` is x then y.
+LayoutBase *make_layout_f32(const fa2_full_params *p, const double *pos, int repulsion);
+LayoutBase *make_layout_f64(const fa2_full_params *p, const double *pos, int repulsion);
+
+struct RepulseBase {
+    virtual ~RepulseBase() {}
+    virtual int exact(const double *x, const double *y, const double *mass,
+                      const double *size, double scaling, double *dx, double *dy) = 0;
+    virtual int bh(const fa2_tree *t, double scaling, double theta, double *dx,
+                   double *dy) = 0;
+    double t_send = 0.0, t_compute = 0.0, t_fetch = 0.0;
+    int device = 0;
+};
+
+RepulseBase *make_repulse_f32(int device, int n, int adjust, int barnes_hut);
+RepulseBase *make_repulse_f64(int device, int n, int adjust, int barnes_hut);
+
+// Host-side checks of caller data that the kernels index with: 0 if valid,
+// otherwise 1 with the message set.
+int check_csr(int n, const int *inc_off, const int *inc_node);
+int check_quadtree(int n, const fa2_tree *t);
+
+} // namespace fa2cu

@@ -1,0 +1,90 @@
+/*
+ * fa2_cuda.h -- entry points of libfa2cuda.so beyond the package's fa2.h.
+ *
+ * fa2.h holds the interface the package's C code links against; these add a
+ * device-resident layout session (the state of fa2_full_run kept on the GPU
+ * between calls), per-step forces for parity checks, phase timings and tree
+ * introspection. They follow fa2.h's conventions: 0 = success, a message in
+ * fa2_gpu_error() otherwise, every pointer owned by the caller, positions and
+ * forces as x[0..n) then y[0..n).
+ */
+#ifndef FA2_CUDA_H
+#define FA2_CUDA_H
+
+#include <stdint.h>
+
+#include "fa2.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct fa2cu_layout fa2cu_layout;
+
+/* How a resident layout computes the repulsion. */
+enum {
+    FA2CU_REPULSION_BH = 0,    /* Barnes-Hut over the Morton/Karras tree,
+                                  as fa2_full_run (no counterpart: the
+                                  reference's src/gpu_full.c:403-499 loop) */
+    FA2CU_REPULSION_EXACT = 1  /* every pair, as src/forceatlas2.c:278-294 */
+};
+
+/* Upload the graph and the start positions of fa2_full_params once and keep
+ * the layout on the device (positions, forces, tree, FP64 speed state).
+ * p->iterations, p->profile and p->interrupted are not used here. NULL on
+ * error. No reference counterpart: src/gpu_full.c:164-396 inlined in
+ * fa2_full_run. */
+fa2cu_layout *fa2cu_layout_open(const fa2_full_params *p, const double *pos,
+                                int repulsion);
+
+/* Enqueue `iterations` iterations on the layout's stream; returns without
+ * waiting. The speed update runs on the device: no host round trip. */
+int fa2cu_layout_iterate(fa2cu_layout *L, int iterations);
+
+/* Wait for the layout's stream. Returns non-zero with the message of
+ * fa2_full_run (src/gpu_full.c:486-491) if the totals became invalid. */
+int fa2cu_layout_sync(fa2cu_layout *L);
+
+/* Download / replace the positions (x then y, doubles). */
+int fa2cu_layout_positions(fa2cu_layout *L, double *pos);
+int fa2cu_layout_set_positions(fa2cu_layout *L, const double *pos);
+
+/* Forces of one iteration at positions pos (repulsion, gravity, attraction),
+ * into f (x then y). The layout's positions are replaced by pos. */
+int fa2cu_layout_forces(fa2cu_layout *L, const double *pos, double *f);
+
+/* Speed, speed efficiency and the last swing / traction totals (FP64). */
+int fa2cu_layout_speed(fa2cu_layout *L, double state[4]);
+
+/* The layout's CUDA stream (a cudaStream_t), for timing with events. */
+void *fa2cu_layout_stream(fa2cu_layout *L);
+
+/* Run `iterations` iterations phase by phase with CUDA events between the
+ * phases, adding the milliseconds of each to ms[FA2_FULL_NTIMES] (slots of
+ * FA2_FULL_T_*; ms[FA2_FULL_T_TOTAL] gets the sum). */
+int fa2cu_layout_phase_times(fa2cu_layout *L, int iterations, double *ms);
+
+/* The Karras construction at positions pos: Morton keys and node order
+ * (sorted), child / range (2(n-1)), parent (2n-1), and per internal node
+ * (cx, cy, m, size^2) in ni (4(n-1)). Barnes-Hut layouts only. */
+int fa2cu_layout_tree(fa2cu_layout *L, const double *pos, uint32_t *key,
+                      uint32_t *order, int *child, int *range, int *parent,
+                      double *ni);
+
+/* Tree nodes visited and node pairs computed by one Barnes-Hut traversal at
+ * the current positions (an instrumented, untimed variant). */
+int fa2cu_layout_traversal_counts(fa2cu_layout *L, double counts[2]);
+
+/* Bytes of device memory held by the layout. */
+double fa2cu_layout_bytes(const fa2cu_layout *L);
+
+void fa2cu_layout_close(fa2cu_layout *L);
+
+/* Library build description (compile flags and architecture). */
+const char *fa2cu_build_info(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

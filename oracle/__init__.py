@@ -84,6 +84,7 @@ def lib():
         _lib = C.CDLL(LIB)
         _lib.orc_forces.restype = C.c_int
         _lib.orc_layout.restype = C.c_int
+        _lib.orc_layout_trace.restype = C.c_int
         _lib.orc_prepare_large.restype = C.c_int
         for s in ("f", "d"):
             getattr(_lib, f"orc_pipe_forces_{s}").restype = C.c_int
@@ -167,6 +168,23 @@ def layout(n, frm, to, w, pos, size, fixed, iterations, opts: Opts,
     if rc:
         raise RuntimeError(ref_lib().ref_error().decode())
     return out.reshape(2, n).T.copy()
+
+
+def layout_trace(n, frm, to, w, pos, size, fixed, iterations, opts: Opts):
+    """Positions before the first iteration and after each one, as an
+    (iterations + 1, n, 2) array."""
+    frm, to, w = _i32(frm), _i32(to), _f64(w)
+    xy = _pos_cols(pos)
+    size = _f64(size if size is not None else np.ones(n))
+    fixed = _i32(fixed if fixed is not None else np.zeros(n))
+    tr = np.zeros((iterations + 1) * 2 * n)
+    o = opts.c()
+    rc = lib().orc_layout_trace(n, len(frm), iptr(frm), iptr(to), dptr(w),
+                                dptr(xy), dptr(size), iptr(fixed), iterations,
+                                C.byref(o), dptr(tr))
+    if rc:
+        raise RuntimeError("oracle layout failed")
+    return tr.reshape(iterations + 1, 2, n).transpose(0, 2, 1).copy()
 
 
 class QuadTree:

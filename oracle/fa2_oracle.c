@@ -488,9 +488,32 @@ static void attract_node(const int *from, const int *to, const double *w,
     dy[i] = fy;
 }
 
+static int layout_impl(int n, int m, const int *from, const int *to,
+                       const double *w, double *pos, const double *size,
+                       const int *fixed, int iterations, const orc_opts *o,
+                       double *trace);
+
 int orc_layout(int n, int m, const int *from, const int *to, const double *w,
                double *pos, const double *size, const int *fixed,
                int iterations, const orc_opts *o)
+{
+    return layout_impl(n, m, from, to, w, pos, size, fixed, iterations, o,
+                       NULL);
+}
+
+int orc_layout_trace(int n, int m, const int *from, const int *to,
+                     const double *w, double *pos, const double *size,
+                     const int *fixed, int iterations, const orc_opts *o,
+                     double *trace)
+{
+    return layout_impl(n, m, from, to, w, pos, size, fixed, iterations, o,
+                       trace);
+}
+
+static int layout_impl(int n, int m, const int *from, const int *to,
+                       const double *w, double *pos, const double *size,
+                       const int *fixed, int iterations, const orc_opts *o,
+                       double *trace)
 {
     /* src/forceatlas2.c:521-803, the CPU branch (gpu = -1) */
     if (n < 0 || m < 0 || iterations < 0) return 1;
@@ -535,6 +558,7 @@ int orc_layout(int n, int m, const int *from, const int *to, const double *w,
 
     const double coef = o->outbound ? mean : 1.0;
     double speed = 1.0, eff = 1.0;
+    if (trace) memcpy(trace, pos, 2 * nn * sizeof(double));
     for (int it = 0; it < iterations; it++) {
         double *tmp = odx;
         odx = dx;
@@ -619,6 +643,9 @@ int orc_layout(int n, int m, const int *from, const int *to, const double *w,
             x[i] += dx[i] * factor;
             y[i] += dy[i] * factor;
         }
+        if (trace)
+            memcpy(trace + 2 * nn * (size_t) (it + 1), pos,
+                   2 * nn * sizeof(double));
     }
     status = 0;
 out:

@@ -87,6 +87,13 @@ int orc_layout(int n, int m, const int *from, const int *to, const double *w,
                double *pos, const double *size, const int *fixed,
                int iterations, const orc_opts *o);
 
+/* orc_layout that also records the positions before the first iteration
+ * and after each one: trace holds (iterations + 1) * 2n doubles. */
+int orc_layout_trace(int n, int m, const int *from, const int *to,
+                     const double *w, double *pos, const double *size,
+                     const int *fixed, int iterations, const orc_opts *o,
+                     double *trace);
+
 /* The symmetric CSR of C_forceatlas2_large with per-incidence coefficients
  * (src/forceatlas2.c:870-902). off has n+1 entries, inc_node and inc_coef
  * 2m. Returns the number of incidences. */

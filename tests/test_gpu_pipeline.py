@@ -1,0 +1,200 @@
+"""The all-GPU pipeline (Morton codes, radix sort, Karras tree, bottom-up
+centres of mass, stackless Barnes-Hut, attraction, swing, apply) against the
+oracle and the golden fixtures of the reference.
+
+Bars: Morton keys, sorted order (ties by index) and the tree's child /
+range / parent arrays bit-exact in both precisions; per-step forces within
+1e-12 (double) of the oracle computing the same construction, and within
+1e-4 (single, norm-wise relative) of the double-precision forces.
+"""
+import numpy as np
+import pytest
+
+from conftest import rel_err
+from forceatlas2_rc_gb300 import graphs as G
+from forceatlas2_rc_gb300.layout import REPULSION_BH, REPULSION_EXACT, Graph, Layout
+
+pytestmark = pytest.mark.gpu
+
+PREC = {"f": "single", "d": "double"}
+
+
+def make_layout(n, a, b, w, pos, precision="single", repulsion=REPULSION_BH,
+                outbound=False, **kw):
+    g = Graph(n, a, b, w, outbound=outbound)
+    return Layout(g, pos, precision=precision, repulsion=repulsion, **kw)
+
+
+def tree_cases(golden):
+    g = golden
+    yield "pb", g["pb_pos"], g["pb_mass"]
+    yield "pl", np.stack([np.arange(64.0), np.zeros(64)], 1), np.ones(64)
+    yield "p2", np.array([[0.0, 0.0], [1.0, 1.0]]), np.ones(2)
+
+
+@pytest.mark.parametrize("prec", ["f", "d"])
+def test_tree_bit_exact_golden(gpu, golden, prec):
+    """Keys, order, child, range, parent and the regions' (cx, cy, m, size^2)
+    equal the reference's pipeline.cl run on the CPU (tests/golden)."""
+    for tag, pos, m in tree_cases(golden):
+        n = len(pos)
+        a = np.zeros(0, np.int32)
+        g = Graph(n, a, a, np.zeros(0))
+        g.mass = np.ascontiguousarray(m, dtype=np.float64)
+        L = Layout(g, pos, precision=PREC[prec])
+        t = L.tree(pos)
+        for k in ("key", "order", "child", "range", "parent"):
+            np.testing.assert_array_equal(t[k], golden[f"{tag}_{prec}_{k}"],
+                                          err_msg=f"{tag} {k}")
+        np.testing.assert_array_equal(t["ni"], golden[f"{tag}_{prec}_ni"],
+                                      err_msg=f"{tag} ni")
+        L.close()
+
+
+@pytest.mark.parametrize("prec", ["f", "d"])
+@pytest.mark.parametrize("n,dup", [(5000, 500), (70000, 0), (3, 3)])
+def test_tree_bit_exact_oracle(gpu, orc, prec, n, dup):
+    rng = np.random.default_rng(n)
+    pos = rng.uniform(-1e3, 1e3, size=(n, 2))
+    if dup:
+        pos[:dup] = pos[rng.integers(0, min(7, n), dup)]
+    m = rng.integers(1, 20, n).astype(float)
+    a = np.zeros(0, np.int32)
+    g = Graph(n, a, a, np.zeros(0))
+    g.mass = m
+    with Layout(g, pos, precision=PREC[prec]) as L:
+        t = L.tree(pos)
+    r = orc.pipe_build(n, pos, m, prec)
+    for k in ("key", "order", "child", "range", "parent", "ni"):
+        np.testing.assert_array_equal(t[k], r[k], err_msg=k)
+
+
+PIPE_SETS = [dict(), dict(linlog=True, adjust=True, theta=0.5),
+             dict(strong=True, theta=0.0), dict(outbound=True, gravity=0.0)]
+
+
+def _pipe_case(golden):
+    g = golden
+    return g["pb_pos"], g["pb_from"], g["pb_to"], g["pf_w"], g["pf_size"]
+
+
+@pytest.mark.parametrize("k", range(len(PIPE_SETS)))
+def test_pipeline_forces_double_vs_golden(gpu, golden, k):
+    """FP64 per-step forces of the Barnes-Hut pipeline: <= 1e-12 against the
+    reference's own pipeline.cl (double) on the CPU."""
+    pos, a, b, w, s = _pipe_case(golden)
+    n = len(pos)
+    d = dict(PIPE_SETS[k])
+    ob = d.pop("outbound", False)
+    with make_layout(n, a, b, w, pos, "double", outbound=ob, size=s, **d) as L:
+        f = L.forces(pos)
+    want = golden[f"pf_{k}_d"]
+    assert rel_err(f, want) <= 1e-12
+
+
+@pytest.mark.parametrize("k", range(len(PIPE_SETS)))
+def test_pipeline_forces_single(gpu, golden, orc, k):
+    """FP32 per-step forces: close to the float construction of the
+    reference, and within 1e-4 of the double-precision forces."""
+    pos, a, b, w, s = _pipe_case(golden)
+    n = len(pos)
+    d = dict(PIPE_SETS[k])
+    ob = d.pop("outbound", False)
+    with make_layout(n, a, b, w, pos, "single", outbound=ob, size=s, **d) as L:
+        f = L.forces(pos)
+    assert rel_err(f, golden[f"pf_{k}_f"]) <= 1e-5
+    assert rel_err(f, golden[f"pf_{k}_d"]) <= 1e-4
+
+
+@pytest.mark.parametrize("theta", [0.0, 0.5, 1.2])
+def test_pipeline_forces_larger(gpu, orc, theta):
+    """BA graph of 20000 nodes with lognormal weights: double == oracle
+    (<= 1e-12); single vs double <= 1e-4."""
+    n, a, b = G.barabasi_albert(20000, 3, seed=2)
+    w = np.random.default_rng(1).lognormal(0.0, 0.5, len(a))
+    pos = G.uniform_positions(n, 0, 1000, seed=3)
+    go = orc.prepare_large(n, a, b, w)
+    p, keep = orc.full_params(go, theta=theta, scaling=2.0)
+    want_d = orc.pipe_forces(p, pos, "d")
+    with make_layout(n, a, b, w, pos, "double", theta=theta) as L:
+        fd = L.forces(pos)
+    assert rel_err(fd, want_d) <= 1e-12
+    with make_layout(n, a, b, w, pos, "single", theta=theta) as L:
+        ff = L.forces(pos)
+    assert rel_err(ff, orc.pipe_forces(p, pos, "f")) <= 1e-5
+    assert rel_err(ff, want_d) <= 1e-4
+
+
+def test_exact_forces_match_forceatlas2c(gpu, golden):
+    """Exact repulsion + gravity + attraction (FP64) reproduce the
+    reference's recorded per-step forces of src/forceatlas2.c."""
+    from golden.make_golden import OPTION_SETS
+    g = golden
+    n = int(g["cf_n"])
+    a, b, w, size, pos = g["cf_from"], g["cf_to"], g["cf_w"], g["cf_size"], g["cf_pos"]
+    for k, d in enumerate(OPTION_SETS):
+        d = dict(d)
+        kw = dict(scaling=d.pop("scaling", 10.0), gravity=d.pop("gravity", 1.0),
+                  strong=d.pop("strong", False), linlog=d.pop("linlog", False),
+                  adjust=d.pop("adjust", False))
+        ob = d.pop("outbound", False)
+        with make_layout(n, a, b, w, pos, "double", REPULSION_EXACT,
+                         outbound=ob, size=size, **kw) as L:
+            f = L.forces(pos)
+        err = rel_err(f, g[f"cf_{k}_0_None"])
+        assert err <= 1e-12, (k, err)
+
+
+def test_config1_per_step_gate(gpu, orc):
+    """Islands 5 x 30, exact, FP64, scaling 2, gravity 1, 1000 iterations:
+    at every step, the GPU forces at the oracle's positions are within
+    1e-12 of src/forceatlas2.c's."""
+    n, a, b = G.islands(5, 30, 0.3, 2, seed=1)
+    w = np.ones(len(a))
+    pos0 = G.uniform_positions(n, 0.0, 1.0, seed=1)
+    o = orc.Opts(scaling=2.0, gravity=1.0)
+    trace = orc.layout_trace(n, a, b, w, pos0, None, None, 1000, o)
+    worst = 0.0
+    with make_layout(n, a, b, w, pos0, "double", REPULSION_EXACT, scaling=2.0) as L:
+        for t in range(0, 1001):
+            f = L.forces(trace[t])
+            want = orc.forces(n, a, b, w, trace[t], None, o)
+            worst = max(worst, rel_err(f, want))
+    assert worst <= 1e-12, worst
+
+
+@pytest.mark.parametrize("k", range(6))
+def test_exact_trajectory_double(gpu, golden, k):
+    """10 iterations of the exact GPU layout in double == C_forceatlas2
+    (tolerance 1e-9 as test-gpu.R:34-58)."""
+    from golden.make_golden import OPTION_SETS
+    g = golden
+    n = int(g["cf_n"])
+    a, b, w, size, pos = g["cf_from"], g["cf_to"], g["cf_w"], g["cf_size"], g["cf_pos"]
+    d = dict(OPTION_SETS[k])
+    kw = dict(scaling=d.pop("scaling", 10.0), gravity=d.pop("gravity", 1.0),
+              strong=d.pop("strong", False), linlog=d.pop("linlog", False),
+              adjust=d.pop("adjust", False))
+    ob = d.pop("outbound", False)
+    with make_layout(n, a, b, w, pos, "double", REPULSION_EXACT, outbound=ob,
+                     size=size, **kw) as L:
+        L.iterate(10)
+        L.sync()
+        xy = L.positions()
+    want = g[f"cl_{k}_0"]
+    np.testing.assert_allclose(xy, want, rtol=1e-9, atol=1e-9 * np.abs(want).max())
+
+
+def test_fixed_nodes(gpu, golden):
+    g = golden
+    n = int(g["cf_n"])
+    a, b, w, size, pos = g["cf_from"], g["cf_to"], g["cf_w"], g["cf_size"], g["cf_pos"]
+    fixed = g["cl_fixed_mask"]
+    with make_layout(n, a, b, w, pos, "double", REPULSION_EXACT, scaling=10.0,
+                     fixed=fixed) as L:
+        L.iterate(10)
+        L.sync()
+        xy = L.positions()
+    np.testing.assert_array_equal(xy[fixed == 1], pos[fixed == 1])
+    np.testing.assert_allclose(xy, g["cl_fixed"], rtol=1e-9,
+                               atol=1e-9 * np.abs(g["cl_fixed"]).max())
