@@ -488,11 +488,18 @@ __device__ inline void update_speed_dev(SpeedState *st, double tsw, double ttr)
     st->efficiency = eff;
 }
 
+// Up to this many nodes the totals are summed serially in node order, the
+// reference's order (src/forceatlas2.c:770-775): in double precision the
+// speed, hence the whole trajectory, is then the reference's bit for bit.
+// Beyond, a fixed-order tree with compensation (a serial sum would cost
+// more than the rest of the iteration).
+constexpr int SERIAL_TOTALS_MAX = 2048;
+
 template <class R>
 __global__ void __launch_bounds__(256)
 k_swing(int n, const typename RT<R>::R2 *__restrict__ f,
         const typename RT<R>::R2 *__restrict__ fold, const R *__restrict__ mass,
-        const uint8_t *__restrict__ fixed, R *__restrict__ sw,
+        const uint8_t *__restrict__ fixed, R *__restrict__ sw, R *__restrict__ tr,
         double2 *__restrict__ partial, unsigned *__restrict__ ticket,
         SpeedState *__restrict__ st, int *__restrict__ status)
 {
@@ -504,10 +511,12 @@ k_swing(int n, const typename RT<R>::R2 *__restrict__ f,
         const R tx = b.x + a.x, ty = b.y + a.y;
         const R m = mass[i];
         const R s = m * fsqrt(sx * sx + sy * sy);
+        const R t = R(0.5) * m * fsqrt(tx * tx + ty * ty);
         sw[i] = s;
+        if (n <= SERIAL_TOTALS_MAX) tr[i] = t;
         if (fixed && fixed[i]) continue;
         as = __dadd_rn(as, (double) s);
-        at = __dadd_rn(at, (double) (R(0.5) * m * fsqrt(tx * tx + ty * ty)));
+        at = __dadd_rn(at, (double) t);
     }
     as = warp_sum(as);
     at = warp_sum(at);
@@ -532,6 +541,25 @@ k_swing(int n, const typename RT<R>::R2 *__restrict__ f,
     __syncthreads();
     if (!last) return;
     __threadfence();
+    if (n <= SERIAL_TOTALS_MAX) {
+        if (threadIdx.x == 0) {
+            double tsw = 0.0, ttr = 0.0;
+            for (int i = 0; i < n; i++) {
+                if (fixed && fixed[i]) continue;
+                tsw = __dadd_rn(tsw, (double) __ldcg(sw + i));
+                ttr = __dadd_rn(ttr, (double) __ldcg(tr + i));
+            }
+            *ticket = 0u;
+            if (!(tsw == tsw) || !(ttr == ttr)) {
+                atomicOr(status + ST_ERROR, ERR_NAN);
+                st->total_swinging = tsw;
+                st->total_traction = ttr;
+            } else {
+                update_speed_dev(st, tsw, ttr);
+            }
+        }
+        return;
+    }
     double s1 = 0.0, c1 = 0.0, s2 = 0.0, c2 = 0.0;
     for (int k = threadIdx.x; k < (int) gridDim.x; k += blockDim.x) {
         const double2 v = __ldcg(partial + k);

@@ -70,7 +70,7 @@ template <class R> struct Layout : LayoutBase {
     cudaStream_t s = nullptr;
     DevMem mem;
     R2 *pos = nullptr, *f = nullptr, *fold = nullptr;
-    R *mass = nullptr, *size = nullptr, *sw = nullptr;
+    R *mass = nullptr, *size = nullptr, *sw = nullptr, *trac = nullptr;
     uint8_t *fixed = nullptr;
     int *inc_off = nullptr;
     Inc<R> *inc = nullptr;
@@ -114,6 +114,7 @@ template <class R> struct Layout : LayoutBase {
         mass = mem.get<R>(nn);
         size = adjust ? mem.get<R>(nn) : nullptr;
         sw = mem.get<R>(nn);
+        trac = n <= SERIAL_TOTALS_MAX ? mem.get<R>(nn) : nullptr;
         fixed = any_fixed ? mem.get<uint8_t>(nn) : nullptr;
         inc_off = mem.get<int>(nn + 1);
         inc = mem.get<Inc<R>>((size_t) ninc);
@@ -281,7 +282,7 @@ template <class R> struct Layout : LayoutBase {
     }
     void launch_move()
     {
-        k_swing<R><<<nswing, 256, 0, s>>>(n, f, fold, mass, fixed, sw, swing_partial,
+        k_swing<R><<<nswing, 256, 0, s>>>(n, f, fold, mass, fixed, sw, trac, swing_partial,
                                           (unsigned *) (status + ST_TICKET_SWING), st, status);
         k_apply<R><<<ceil_div(n, 256), 256, 0, s>>>(n, adjust, f, fold, sw, fixed, pos, st,
                                                     status);

@@ -2,8 +2,13 @@
 the oracle (src/forceatlas2.c restated; pinned by tests/golden).
 
 Tolerances (per-step force, norm-wise relative error
-max_i |f_i - g_i| / max_i |g_i|): precision "double" <= 1e-12 (the FP64
-kernels keep the reference's operation order), precision "single" <= 1e-4.
+max_i |f_i - g_i| / max_i |g_i|, from identical positions): precision
+"double" <= 1e-12 (the FP64 kernels keep the reference's operation order),
+precision "single" <= 1e-4. With prevent_overlap (adjust) the single bar is
+2e-3: near contact, d = sqrt(d2) - (r_i + r_j) cancels and float inputs carry
+an absolute error of about one ulp of the coordinates, so the condition
+number of the force grows like r / d (the reference's float construction
+shows 2e-4 on these cases).
 """
 import ctypes as C
 
@@ -17,6 +22,16 @@ from forceatlas2_rc_gb300._abi import dptr
 pytestmark = pytest.mark.gpu
 
 TOL = {1: 1e-12, 0: 1e-4}
+TOL_ADJUST_SINGLE = 2e-3
+
+
+def tol(use_double, adjust):
+    return TOL[1] if use_double else (TOL_ADJUST_SINGLE if adjust else TOL[0])
+
+
+def f32(a):
+    """Values the single-precision path represents exactly."""
+    return None if a is None else np.asarray(a).astype(np.float32).astype(np.float64)
 
 
 def _case(n, seed=42, coincident=0):
@@ -43,6 +58,8 @@ class Session:
 @pytest.mark.parametrize("adjust", [0, 1])
 def test_repulse_exact(cuda_lib, gpu, orc, use_double, adjust):
     n, a, b, size, pos = _case(400, coincident=10)
+    if not use_double:
+        pos, size = f32(pos), f32(size)
     m, _ = orc.mass(n, a, b)
     want = orc.repulse_exact(n, pos, m, size if adjust else None, adjust, 5.0)
     s = Session(cuda_lib, n, use_double, adjust, 0)
@@ -58,7 +75,7 @@ def test_repulse_exact(cuda_lib, gpu, orc, use_double, adjust):
     call()
     got = np.stack([dx, dy], axis=1)
     err = rel_err(got, want)
-    assert err <= TOL[use_double], err
+    assert err <= tol(use_double, adjust), err
     if use_double:
         # same operations in the same order as the reference
         np.testing.assert_array_equal(got, want)
@@ -75,6 +92,8 @@ def test_repulse_exact(cuda_lib, gpu, orc, use_double, adjust):
 @pytest.mark.parametrize("adjust", [0, 1])
 def test_repulse_bh_quadtree(cuda_lib, gpu, orc, use_double, theta, adjust):
     n, a, b, size, pos = _case(500, coincident=25)
+    if not use_double:
+        pos, size = f32(pos), f32(size)
     m, _ = orc.mass(n, a, b)
     sz = size if adjust else None
     qt = orc.QuadTree(n, pos, m, sz)
@@ -86,7 +105,7 @@ def test_repulse_bh_quadtree(cuda_lib, gpu, orc, use_double, theta, adjust):
     assert rc == 0, cuda_lib.fa2_gpu_error()
     got = np.stack([dx, dy], axis=1)
     err = rel_err(got, want)
-    assert err <= TOL[use_double], err
+    assert err <= tol(use_double, adjust), err
     if use_double:
         np.testing.assert_array_equal(got, want)
     s.close()
