@@ -204,6 +204,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--profile-only", action="store_true",
                     help="warm-up and a few iterations only (for ncu)")
+    ap.add_argument("--walk", default="warp", choices=["warp", "thread"],
+                    help="Barnes-Hut walk (identical forces)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -227,6 +229,8 @@ def main():
     g = Graph(n, a, b, np.ones(len(a)), outbound=True)
     kw = dict(scaling=2.0, gravity=1.0, theta=1.2, linlog=True, device=local)
     L = Layout(g, pos, precision="single", repulsion=REPULSION_BH, **kw)
+    if args.walk == "thread":
+        L.option("walk", 1)
     stream = torch.cuda.ExternalStream(L.stream, device=local)
 
     if args.profile_only:
@@ -351,7 +355,8 @@ def main():
     l2_bytes = 32.0 * counts["visits"] + 16.0 * counts["pairs"]
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"],
                 "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"],
-                "traffic": None, "kernel": "k_traverse<float>",
+                "traffic": None,
+                "kernel": "k_traverse_warp<float>" if args.walk == "warp" else "k_traverse<float>",
                 "peak_kind": f"{kind} (HBM copy)",
                 "launch_ms": ph["repulsion"],
                 "l2_request_bytes": l2_bytes,
@@ -375,7 +380,8 @@ def main():
         "data": "synthetic",
         "config": {"workload": WORKLOAD, "n": n, "edges": int(len(a)),
                    "parallelism": "replicas" if ws > 1 else "single GPU",
-                   "l2": "working set > 129 MB L2 (no flush needed)"},
+                   "l2": "working set > 129 MB L2 (no flush needed)",
+                "walk": args.walk},
         "fp64_value": fp64_value,
         "fp32_over_fp64": value / ws / fp64_value,
         "force_err_fp32_vs_fp64": force_err,

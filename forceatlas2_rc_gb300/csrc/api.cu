@@ -330,6 +330,14 @@ int fa2cu_layout_traversal_counts(fa2cu_layout *L, double counts[2])
 {
     return L->impl->traversal_counts(counts);
 }
+int fa2cu_layout_option(fa2cu_layout *L, const char *name, double value)
+{
+    if (!name) {
+        set_message("invalid option");
+        return 1;
+    }
+    return L->impl->option(name, value);
+}
 double fa2cu_layout_bytes(const fa2cu_layout *L) { return L->impl->bytes(); }
 void fa2cu_layout_close(fa2cu_layout *L)
 {

@@ -23,6 +23,9 @@ void set_cuda_error(const char *what, cudaError_t e);
         }                                                                      \
     } while (0)
 
+// Barnes-Hut walk variants (both give identical forces).
+enum { WALK_WARP = 0, WALK_THREAD = 1 };
+
 // Device-side status words (one int each in a session's `status` buffer).
 enum {
     ST_ERROR = 0,      // non-zero: a kernel gave up; bit values below
@@ -72,9 +75,23 @@ template <class R> struct alignas(2 * sizeof(R) > 8 ? 16 : 8) Inc {
     R coef;
 };
 
-// Per-node sum over the internal nodes of the tree (bbox, mass, m*x, m*y).
-template <class R> struct alignas(sizeof(R) * 8) Agg {
-    R minx, miny, maxx, maxy, m, mx, my, pad;
+// Per-region sums of the tree: bounding box, mass, sum m*x and sum m*y.
+// Summed in plain float, sum m*x over a million nodes at coordinates ~1e4
+// loses the centre of mass to ~1e-2 (the reference's float construction
+// does). The FP64 path sums in double; the FP32 path in float-float (an
+// unevaluated pair hi + lo kept exact by error-free transformations), which
+// is as accurate for these sums and stays on the FP32 pipe (GB300's FP64
+// rate is 1/64 of its FP32 rate).
+struct ff2 {
+    float hi, lo;
+};
+template <class R> struct Agg;
+template <> struct alignas(32) Agg<double> {
+    double minx, miny, maxx, maxy, m, mx, my, pad;
+};
+template <> struct alignas(16) Agg<float> {
+    float minx, miny, maxx, maxy;
+    ff2 m, mx, my, pad;
 };
 
 // Leaves of a device-side quadtree region list (fa2_gpu_repulse_bh):

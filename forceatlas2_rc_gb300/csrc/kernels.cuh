@@ -82,7 +82,7 @@ template <class T> __device__ __forceinline__ T warp_sum(T v)
 template <class R>
 __global__ void __launch_bounds__(256)
 k_bbox(int n, const typename RT<R>::R2 *__restrict__ pos, R *__restrict__ partial,
-       R *__restrict__ bbox, unsigned *__restrict__ ticket)
+       R *__restrict__ bbox, double *__restrict__ quant, unsigned *__restrict__ ticket)
 {
     typedef typename RT<R>::R2 R2;
     R mnx, mny, mxx, mxy;
@@ -133,20 +133,47 @@ k_bbox(int n, const typename RT<R>::R2 *__restrict__ pos, R *__restrict__ partia
     }
     __syncthreads();
     if (!last) return;
+    // the last block reduces the partials, every thread a strided share
+    __threadfence();
+    R a = __ldcg(partial), b = __ldcg(partial + 1), c = __ldcg(partial + 2),
+      d = __ldcg(partial + 3);
+    for (int k = threadIdx.x; k < (int) gridDim.x; k += blockDim.x) {
+        a = cl_min(a, __ldcg(partial + 4 * k));
+        b = cl_min(b, __ldcg(partial + 4 * k + 1));
+        c = cl_max(c, __ldcg(partial + 4 * k + 2));
+        d = cl_max(d, __ldcg(partial + 4 * k + 3));
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        a = cl_min(a, __shfl_down_sync(0xffffffffu, a, o));
+        b = cl_min(b, __shfl_down_sync(0xffffffffu, b, o));
+        c = cl_max(c, __shfl_down_sync(0xffffffffu, c, o));
+        d = cl_max(d, __shfl_down_sync(0xffffffffu, d, o));
+    }
+    __syncthreads();
+    if (lane == 0) {
+        s[0][w] = a;
+        s[1][w] = b;
+        s[2][w] = c;
+        s[3][w] = d;
+    }
+    __syncthreads();
     if (threadIdx.x == 0) {
-        __threadfence();
-        R a = __ldcg(partial), b = __ldcg(partial + 1), c = __ldcg(partial + 2),
-          d = __ldcg(partial + 3);
-        for (int k = 1; k < (int) gridDim.x; k++) {
-            a = cl_min(a, __ldcg(partial + 4 * k));
-            b = cl_min(b, __ldcg(partial + 4 * k + 1));
-            c = cl_max(c, __ldcg(partial + 4 * k + 2));
-            d = cl_max(d, __ldcg(partial + 4 * k + 3));
+        for (int k = 1; k < (int) (blockDim.x >> 5); k++) {
+            a = cl_min(a, s[0][k]);
+            b = cl_min(b, s[1][k]);
+            c = cl_max(c, s[2][k]);
+            d = cl_max(d, s[3][k]);
         }
         bbox[0] = a;
         bbox[1] = b;
         bbox[2] = c;
         bbox[3] = d;
+        // the Morton quantisation of pipeline.cl:122-124, in double
+        const double w = __dsub_rn((double) c, (double) a), h = __dsub_rn((double) d, (double) b);
+        const double extent = cl_max(w, h);
+        quant[0] = (double) a;
+        quant[1] = (double) b;
+        quant[2] = extent > 0.0 ? __ddiv_rn(65535.0, extent) : 0.0;
         *ticket = 0u;
     }
 }
@@ -163,20 +190,23 @@ __device__ __forceinline__ uint32_t spread16(uint32_t v)
     return v;
 }
 
+// The quantisation runs in double in both precisions (float coordinates
+// widen exactly), so that a layout's tree depends on its positions only, not
+// on the precision of the iteration: the FP32 path builds the tree of the
+// reference's double construction.
 template <class R>
 __global__ void __launch_bounds__(256)
-k_morton(int n, const typename RT<R>::R2 *__restrict__ pos, const R *__restrict__ bbox,
+k_morton(int n, const typename RT<R>::R2 *__restrict__ pos, const double *__restrict__ quant,
          uint32_t *__restrict__ key, uint32_t *__restrict__ idx)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const R minx = bbox[0], miny = bbox[1];
-    const R w = rsub(bbox[2], minx), h = rsub(bbox[3], miny);
-    const R extent = cl_max(w, h);
-    const R scale = extent > R(0) ? rdiv(R(65535), extent) : R(0);
+    const double minx = quant[0], miny = quant[1], scale = quant[2];
     const typename RT<R>::R2 p = pos[i];
-    const R fx = cl_min(cl_max(rmul(rsub(p.x, minx), scale), R(0)), R(65535));
-    const R fy = cl_min(cl_max(rmul(rsub(p.y, miny), scale), R(0)), R(65535));
+    const double fx =
+        cl_min(cl_max(__dmul_rn(__dsub_rn((double) p.x, minx), scale), 0.0), 65535.0);
+    const double fy =
+        cl_min(cl_max(__dmul_rn(__dsub_rn((double) p.y, miny), scale), 0.0), 65535.0);
     key[i] = spread16((uint32_t) fx) | (spread16((uint32_t) fy) << 1);
     idx[i] = (uint32_t) i;
 }
@@ -209,33 +239,161 @@ k_gather(int n, int adjust, const uint32_t *__restrict__ order,
 // thread ever waits. The region's traversal record gets its skip link:
 // rope[last] is the right child of the region split just after `last`.
 
-template <class R>
-__device__ __forceinline__ Agg<R> leaf_agg(const typename RT<R>::R4 &p)
+// ---- float-float arithmetic (error-free transformations) ------------------
+
+__device__ __forceinline__ ff2 ff_from(float a) { return ff2{a, 0.0f}; }
+
+// (a.hi + a.lo) + (b.hi + b.lo), renormalised; never fused or reassociated.
+__device__ __forceinline__ ff2 ff_add(ff2 a, ff2 b)
 {
-    Agg<R> a;
+    const float s = __fadd_rn(a.hi, b.hi);
+    const float bb = __fsub_rn(s, a.hi);
+    float e = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, bb)), __fsub_rn(b.hi, bb));
+    e = __fadd_rn(e, __fadd_rn(a.lo, b.lo));
+    const float hi = __fadd_rn(s, e);
+    return ff2{hi, __fsub_rn(e, __fsub_rn(hi, s))};
+}
+
+// x * y exactly, as hi + lo (the error term of the product by FMA).
+__device__ __forceinline__ ff2 ff_mul(float x, float y)
+{
+    const float p = __fmul_rn(x, y);
+    return ff2{p, __fmaf_rn(x, y, -p)};
+}
+
+__device__ __forceinline__ double ff_to_double(ff2 a) { return (double) a.hi + (double) a.lo; }
+
+// ---- per-region sums, in the precision of each path ------------------------
+
+__device__ __forceinline__ Agg<double> leaf_agg(const double4_32a &p)
+{
+    Agg<double> a;
     a.minx = a.maxx = p.x;
     a.miny = a.maxy = p.y;
     a.m = p.z;
-    a.mx = rmul(p.x, p.z);
-    a.my = rmul(p.y, p.z);
-    a.pad = R(0);
+    a.mx = __dmul_rn(p.x, p.z);
+    a.my = __dmul_rn(p.y, p.z);
+    a.pad = 0.0;
     return a;
 }
 
-template <class R>
-__device__ __forceinline__ Agg<R> load_agg_cg(const Agg<R> *a)
+__device__ __forceinline__ Agg<float> leaf_agg(const float4 &p)
 {
-    Agg<R> v;
-    const R *p = reinterpret_cast<const R *>(a);
-    v.minx = __ldcg(p);
-    v.miny = __ldcg(p + 1);
-    v.maxx = __ldcg(p + 2);
-    v.maxy = __ldcg(p + 3);
-    v.m = __ldcg(p + 4);
-    v.mx = __ldcg(p + 5);
-    v.my = __ldcg(p + 6);
-    v.pad = R(0);
+    Agg<float> a;
+    a.minx = a.maxx = p.x;
+    a.miny = a.maxy = p.y;
+    a.m = ff_from(p.z);
+    a.mx = ff_mul(p.x, p.z);
+    a.my = ff_mul(p.y, p.z);
+    a.pad = ff2{0.0f, 0.0f};
+    return a;
+}
+
+__device__ __forceinline__ Agg<double> load_agg_cg(const Agg<double> *a)
+{
+    Agg<double> v;
+    const double2 *p = reinterpret_cast<const double2 *>(a);
+    const double2 q0 = __ldcg(p), q1 = __ldcg(p + 1), q2 = __ldcg(p + 2), q3 = __ldcg(p + 3);
+    v.minx = q0.x;
+    v.miny = q0.y;
+    v.maxx = q1.x;
+    v.maxy = q1.y;
+    v.m = q2.x;
+    v.mx = q2.y;
+    v.my = q3.x;
+    v.pad = 0.0;
     return v;
+}
+
+__device__ __forceinline__ Agg<float> load_agg_cg(const Agg<float> *a)
+{
+    Agg<float> v;
+    const float4 *p = reinterpret_cast<const float4 *>(a);
+    const float4 q0 = __ldcg(p), q1 = __ldcg(p + 1), q2 = __ldcg(p + 2);
+    v.minx = q0.x;
+    v.miny = q0.y;
+    v.maxx = q0.z;
+    v.maxy = q0.w;
+    v.m = ff2{q1.x, q1.y};
+    v.mx = ff2{q1.z, q1.w};
+    v.my = ff2{q2.x, q2.y};
+    v.pad = ff2{0.0f, 0.0f};
+    return v;
+}
+
+// The region from its two children, a then b (the order does not depend on
+// which child arrives last).
+__device__ __forceinline__ Agg<double> agg_combine(const Agg<double> &a, const Agg<double> &b)
+{
+    Agg<double> q;
+    q.minx = cl_min(a.minx, b.minx);
+    q.miny = cl_min(a.miny, b.miny);
+    q.maxx = cl_max(a.maxx, b.maxx);
+    q.maxy = cl_max(a.maxy, b.maxy);
+    q.m = __dadd_rn(a.m, b.m);
+    q.mx = __dadd_rn(a.mx, b.mx);
+    q.my = __dadd_rn(a.my, b.my);
+    q.pad = 0.0;
+    return q;
+}
+
+__device__ __forceinline__ Agg<float> agg_combine(const Agg<float> &a, const Agg<float> &b)
+{
+    Agg<float> q;
+    q.minx = cl_min(a.minx, b.minx);
+    q.miny = cl_min(a.miny, b.miny);
+    q.maxx = cl_max(a.maxx, b.maxx);
+    q.maxy = cl_max(a.maxy, b.maxy);
+    q.m = ff_add(a.m, b.m);
+    q.mx = ff_add(a.mx, b.mx);
+    q.my = ff_add(a.my, b.my);
+    q.pad = ff2{0.0f, 0.0f};
+    return q;
+}
+
+// (cx, cy, m, size^2) of a region: the reference's finalize
+// (pipeline.cl:312-323); in double for the FP64 path, from the float-float
+// sums for the FP32 path.
+__device__ __forceinline__ double4_32a agg_record(const Agg<double> &q)
+{
+    const double w = __dsub_rn(q.maxx, q.minx), h = __dsub_rn(q.maxy, q.miny);
+    double4_32a c;
+    c.x = __ddiv_rn(q.mx, q.m);
+    c.y = __ddiv_rn(q.my, q.m);
+    c.z = q.m;
+    c.w = __dmul_rn(2.0, __dadd_rn(__dmul_rn(w, w), __dmul_rn(h, h)));
+    return c;
+}
+
+__device__ __forceinline__ float4 agg_record(const Agg<float> &q)
+{
+    const float m = q.m.hi + q.m.lo;
+    const float w = q.maxx - q.minx, h = q.maxy - q.miny;
+    return make_float4(__fdiv_rn(q.mx.hi + q.mx.lo, m), __fdiv_rn(q.my.hi + q.my.lo, m), m,
+                       2.0f * (w * w + h * h));
+}
+
+// The opening test of the double construction, for a region of either path.
+__device__ __forceinline__ bool far_fp64(const Agg<double> &q, double xi, double yi,
+                                         double theta2d)
+{
+    const double4_32a c = agg_record(q);
+    const double xd = __dsub_rn(xi, c.x), yd = __dsub_rn(yi, c.y);
+    const double d2 = __dadd_rn(__dmul_rn(xd, xd), __dmul_rn(yd, yd));
+    return __dmul_rn(d2, theta2d) > c.w;
+}
+
+__device__ __forceinline__ bool far_fp64(const Agg<float> &q, double xi, double yi,
+                                         double theta2d)
+{
+    const double m = ff_to_double(q.m);
+    const double cx = __ddiv_rn(ff_to_double(q.mx), m), cy = __ddiv_rn(ff_to_double(q.my), m);
+    const double w = __dsub_rn((double) q.maxx, (double) q.minx);
+    const double h = __dsub_rn((double) q.maxy, (double) q.miny);
+    const double s2 = __dmul_rn(2.0, __dadd_rn(__dmul_rn(w, w), __dmul_rn(h, h)));
+    const double xd = __dsub_rn(xi, cx), yd = __dsub_rn(yi, cy);
+    const double d2 = __dadd_rn(__dmul_rn(xd, xd), __dmul_rn(yd, yd));
+    return __dmul_rn(d2, theta2d) > s2;
 }
 
 template <class R>
@@ -264,23 +422,13 @@ k_aggregate(int n, const typename RT<R>::R4 *__restrict__ psort,
             atomicOr(status + ST_ERROR, ERR_BOUNDS);
             return;
         }
-        const Agg<R> a = c.x >= nl ? leaf_agg<R>(psort[c.x - nl]) : load_agg_cg(agg + c.x);
-        const Agg<R> b = c.y >= nl ? leaf_agg<R>(psort[c.y - nl]) : load_agg_cg(agg + c.y);
-        Agg<R> q;
-        q.minx = cl_min(a.minx, b.minx);
-        q.miny = cl_min(a.miny, b.miny);
-        q.maxx = cl_max(a.maxx, b.maxx);
-        q.maxy = cl_max(a.maxy, b.maxy);
-        q.m = radd(a.m, b.m);
-        q.mx = radd(a.mx, b.mx);
-        q.my = radd(a.my, b.my);
-        q.pad = R(0);
+        const Agg<R> a = c.x >= nl ? leaf_agg(psort[c.x - nl]) : load_agg_cg(agg + c.x);
+        const Agg<R> b = c.y >= nl ? leaf_agg(psort[c.y - nl]) : load_agg_cg(agg + c.y);
+        const Agg<R> q = agg_combine(a, b);
         agg[r] = q;
-        const R w = rsub(q.maxx, q.minx), h = rsub(q.maxy, q.miny);
         const int2 rg = range[r];
         BHNode<R> nd;
-        nd.c = mk4<R>(rdiv(q.mx, q.m), rdiv(q.my, q.m), q.m,
-                      rmul(R(2), radd(rmul(w, w), rmul(h, h))));
+        nd.c = agg_record(q);
         nd.t = make_int4(c.x, rope[rg.y], rg.x, rg.y);
         nodes[r] = nd;
         r = parent[r];
@@ -295,12 +443,20 @@ k_aggregate(int n, const typename RT<R>::R4 *__restrict__ psort,
 // node; each step of the loop handles either one region or one node pair, so
 // the threads of a warp stay in step.
 
+// In float, a region whose test d^2 theta^2 > size^2 lands within 1e-4 of
+// the boundary is decided again in double, from the region's double sums:
+// the float path then approximates exactly the regions the double path
+// approximates (a flipped decision would change a node's force by the
+// approximation error itself, ~1e-2 of that region's pull).
+constexpr float DECIDE_BAND = 1e-4f;
+
 template <class R, bool ADJUST>
 __global__ void __launch_bounds__(256)
-k_traverse(int n, R scaling, R theta2, const typename RT<R>::R4 *__restrict__ psort,
-           const BHNode<R> *__restrict__ nodes, const int *__restrict__ rope,
-           const uint32_t *__restrict__ order, typename RT<R>::R2 *__restrict__ f,
-           int *__restrict__ status)
+k_traverse(int n, R scaling, R theta2, double theta2d,
+           const typename RT<R>::R4 *__restrict__ psort,
+           const BHNode<R> *__restrict__ nodes, const Agg<R> *__restrict__ agg,
+           const int *__restrict__ rope, const uint32_t *__restrict__ order,
+           typename RT<R>::R2 *__restrict__ f, int *__restrict__ status)
 {
     typedef typename RT<R>::R4 R4;
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -339,7 +495,11 @@ k_traverse(int n, R scaling, R theta2, const typename RT<R>::R4 *__restrict__ ps
         const BHNode<R> nd = nodes[cur];
         const R xd = xi - nd.c.x, yd = yi - nd.c.y;
         const R d2 = xd * xd + yd * yd;
-        if (d2 * theta2 > nd.c.w) {
+        const R lhs = d2 * theta2;
+        bool far = lhs > nd.c.w;
+        if (sizeof(R) == 4 && fabs(lhs - nd.c.w) <= R(DECIDE_BAND) * nd.c.w)
+            far = far_fp64(agg[cur], (double) xi, (double) yi, theta2d);
+        if (far) {
             const R g = fdiv(scaling * (mi * nd.c.z), d2);
             ax += xd * g;
             ay += yd * g;
@@ -355,13 +515,99 @@ k_traverse(int n, R scaling, R theta2, const typename RT<R>::R4 *__restrict__ ps
     f[order[k]] = mk2<R>(ax, ay);
 }
 
+// The same walk, warp-synchronous. The 32 threads of a warp (neighbours in
+// Morton order) walk the tree together, one region per step, so that every
+// load is a broadcast and no branch diverges; a region is opened when any
+// lane needs it opened. Each lane keeps its own decisions: after it
+// approximates a region (or sums its small range), the lane stays inactive
+// until the walk reaches the first region past that region's subtree --
+// in preorder the first region whose first sorted node is `last + 1`. A lane
+// therefore computes exactly the interactions of the per-thread walk, in the
+// same order, with the same arithmetic: the forces are identical.
+template <class R, bool ADJUST>
+__global__ void __launch_bounds__(256)
+k_traverse_warp(int n, R scaling, R theta2, double theta2d,
+                const typename RT<R>::R4 *__restrict__ psort,
+                const BHNode<R> *__restrict__ nodes, const Agg<R> *__restrict__ agg,
+                const int *__restrict__ rope, const uint32_t *__restrict__ order,
+                typename RT<R>::R2 *__restrict__ f, int *__restrict__ status)
+{
+    typedef typename RT<R>::R4 R4;
+    const unsigned FULL = 0xffffffffu;
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if ((k & ~31) >= n) return; // whole warp past the end
+    const bool valid = k < n;
+    const R4 me = psort[valid ? k : n - 1];
+    const R xi = me.x, yi = me.y, mi = me.z, si = me.w;
+    R ax = R(0), ay = R(0);
+    const int nl = n - 1;
+    // active while the current region's first sorted node is >= resume
+    int resume = valid ? 0 : 0x7fffffff;
+    int cur = 0; // uniform across the warp
+    const int cap = 2 * n + 64;
+    for (int step = 0; cur >= 0; step++) {
+        if (step > cap || cur >= nl + n) { // uniform
+            if ((threadIdx.x & 31) == 0) atomicOr(status + ST_ERROR, ERR_BOUNDS);
+            break;
+        }
+        if (cur >= nl) { // a single node
+            const int j = cur - nl;
+            if (j >= resume && j != k) {
+                const R4 q = psort[j];
+                const R xd = xi - q.x, yd = yi - q.y;
+                const R g = rep_factor<R, ADJUST>(xd * xd + yd * yd, mi * q.z, si + q.w,
+                                                  scaling);
+                ax += xd * g;
+                ay += yd * g;
+            }
+            cur = rope[j];
+            continue;
+        }
+        const BHNode<R> nd = nodes[cur];
+        bool open = false, direct = false;
+        if (nd.t.z >= resume) {
+            const R xd = xi - nd.c.x, yd = yi - nd.c.y;
+            const R d2 = xd * xd + yd * yd;
+            const R lhs = d2 * theta2;
+            bool far = lhs > nd.c.w;
+            if (sizeof(R) == 4 && fabs(lhs - nd.c.w) <= R(DECIDE_BAND) * nd.c.w)
+                far = far_fp64(agg[cur], (double) xi, (double) yi, theta2d);
+            if (far) {
+                const R g = fdiv(scaling * (mi * nd.c.z), d2);
+                ax += xd * g;
+                ay += yd * g;
+                resume = nd.t.w + 1;
+            } else if (nd.t.w - nd.t.z >= 8) {
+                open = true;
+            } else {
+                direct = true;
+                resume = nd.t.w + 1;
+            }
+        }
+        if (__any_sync(FULL, direct)) {
+            for (int j = nd.t.z; j <= nd.t.w; j++) {
+                const R4 q = psort[j];
+                if (direct && j != k) {
+                    const R xd = xi - q.x, yd = yi - q.y;
+                    const R g = rep_factor<R, ADJUST>(xd * xd + yd * yd, mi * q.z, si + q.w,
+                                                      scaling);
+                    ax += xd * g;
+                    ay += yd * g;
+                }
+            }
+        }
+        cur = __any_sync(FULL, open) ? nd.t.x : nd.t.y;
+    }
+    if (valid) f[order[k]] = mk2<R>(ax, ay);
+}
+
 // Instrumented copy of the walk: counts regions visited and node pairs
 // computed (for the traffic estimate of the roofline; never timed).
 template <class R>
 __global__ void __launch_bounds__(256)
-k_traverse_count(int n, R theta2, const typename RT<R>::R4 *__restrict__ psort,
-                 const BHNode<R> *__restrict__ nodes, const int *__restrict__ rope,
-                 unsigned long long *__restrict__ counts)
+k_traverse_count(int n, R theta2, double theta2d, const typename RT<R>::R4 *__restrict__ psort,
+                 const BHNode<R> *__restrict__ nodes, const Agg<R> *__restrict__ agg,
+                 const int *__restrict__ rope, unsigned long long *__restrict__ counts)
 {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     unsigned long long visits = 0, pairs = 0;
@@ -379,7 +625,11 @@ k_traverse_count(int n, R theta2, const typename RT<R>::R4 *__restrict__ psort,
             const BHNode<R> nd = nodes[cur];
             const R xd = me.x - nd.c.x, yd = me.y - nd.c.y;
             const R d2 = xd * xd + yd * yd;
-            if (d2 * theta2 > nd.c.w) {
+            const R lhs = d2 * theta2;
+            bool far = lhs > nd.c.w;
+            if (sizeof(R) == 4 && fabs(lhs - nd.c.w) <= R(DECIDE_BAND) * nd.c.w)
+                far = far_fp64(agg[cur], (double) me.x, (double) me.y, theta2d);
+            if (far) {
                 cur = nd.t.y;
             } else if (nd.t.w - nd.t.z >= 8) {
                 cur = nd.t.x;
@@ -503,6 +753,9 @@ k_swing(int n, const typename RT<R>::R2 *__restrict__ f,
         double2 *__restrict__ partial, unsigned *__restrict__ ticket,
         SpeedState *__restrict__ st, int *__restrict__ status)
 {
+    // per thread: in float-float (FP32 path) or double (FP64 path), over a
+    // fixed set of nodes
+    ff2 fs = ff_from(0.0f), ft = ff_from(0.0f);
     double as = 0.0, at = 0.0;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n;
          i += gridDim.x * blockDim.x) {
@@ -515,11 +768,28 @@ k_swing(int n, const typename RT<R>::R2 *__restrict__ f,
         sw[i] = s;
         if (n <= SERIAL_TOTALS_MAX) tr[i] = t;
         if (fixed && fixed[i]) continue;
-        as = __dadd_rn(as, (double) s);
-        at = __dadd_rn(at, (double) t);
+        if constexpr (sizeof(R) == 4) {
+            fs = ff_add(fs, ff_from((float) s));
+            ft = ff_add(ft, ff_from((float) t));
+        } else {
+            as = __dadd_rn(as, (double) s);
+            at = __dadd_rn(at, (double) t);
+        }
     }
-    as = warp_sum(as);
-    at = warp_sum(at);
+    // per warp and per block, in a fixed tree order
+    if constexpr (sizeof(R) == 4) {
+        for (int o = 16; o > 0; o >>= 1) {
+            fs = ff_add(fs, ff2{__shfl_down_sync(0xffffffffu, fs.hi, o),
+                                __shfl_down_sync(0xffffffffu, fs.lo, o)});
+            ft = ff_add(ft, ff2{__shfl_down_sync(0xffffffffu, ft.hi, o),
+                                __shfl_down_sync(0xffffffffu, ft.lo, o)});
+        }
+        as = ff_to_double(fs);
+        at = ff_to_double(ft);
+    } else {
+        as = warp_sum(as);
+        at = warp_sum(at);
+    }
     __shared__ double ss[8], st_[8];
     __shared__ int last;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -529,12 +799,12 @@ k_swing(int n, const typename RT<R>::R2 *__restrict__ f,
     }
     __syncthreads();
     if (threadIdx.x == 0) {
-        double a = 0.0, b = 0.0;
+        double a = 0.0, b = 0.0, ca = 0.0, cb = 0.0;
         for (int k = 0; k < (int) (blockDim.x >> 5); k++) {
-            a = __dadd_rn(a, ss[k]);
-            b = __dadd_rn(b, st_[k]);
+            neumaier(a, ca, ss[k]);
+            neumaier(b, cb, st_[k]);
         }
-        partial[blockIdx.x] = make_double2(a, b);
+        partial[blockIdx.x] = make_double2(__dadd_rn(a, ca), __dadd_rn(b, cb));
         __threadfence();
         last = atomicAdd(ticket, 1u) == gridDim.x - 1;
     }
@@ -560,21 +830,28 @@ k_swing(int n, const typename RT<R>::R2 *__restrict__ f,
         }
         return;
     }
+    // the block partials: compensated per thread (strided, fixed), then a
+    // fixed tree over the threads
     double s1 = 0.0, c1 = 0.0, s2 = 0.0, c2 = 0.0;
     for (int k = threadIdx.x; k < (int) gridDim.x; k += blockDim.x) {
         const double2 v = __ldcg(partial + k);
         neumaier(s1, c1, v.x);
         neumaier(s2, c2, v.y);
     }
-    __shared__ double r1[256], r2[256];
-    r1[threadIdx.x] = __dadd_rn(s1, c1);
-    r2[threadIdx.x] = __dadd_rn(s2, c2);
+    double v1 = __dadd_rn(s1, c1), v2 = __dadd_rn(s2, c2);
+    v1 = warp_sum(v1);
+    v2 = warp_sum(v2);
+    __syncthreads();
+    if (lane == 0) {
+        ss[w] = v1;
+        st_[w] = v2;
+    }
     __syncthreads();
     if (threadIdx.x == 0) {
         double t1 = 0.0, k1 = 0.0, t2 = 0.0, k2 = 0.0;
-        for (int k = 0; k < (int) blockDim.x; k++) {
-            neumaier(t1, k1, r1[k]);
-            neumaier(t2, k2, r2[k]);
+        for (int k = 0; k < (int) (blockDim.x >> 5); k++) {
+            neumaier(t1, k1, ss[k]);
+            neumaier(t2, k2, st_[k]);
         }
         const double tsw = __dadd_rn(t1, k1), ttr = __dadd_rn(t2, k2);
         *ticket = 0u;
@@ -882,8 +1159,9 @@ k_qregions(int nreg, const fa2_region *__restrict__ reg, QRegion<R> *__restrict_
 // output is in tree order too.
 template <class R, bool ADJUST>
 __global__ void __launch_bounds__(256)
-k_qtraverse(int n, R scaling, R theta2, const typename RT<R>::R4 *__restrict__ p,
-            const QRegion<R> *__restrict__ reg, int nreg,
+k_qtraverse(int n, R scaling, R theta2, double theta2d, const typename RT<R>::R4 *__restrict__ p,
+            const double *__restrict__ px, const double *__restrict__ py,
+            const QRegion<R> *__restrict__ reg, const fa2_region *__restrict__ raw, int nreg,
             typename RT<R>::R2 *__restrict__ f, int *__restrict__ status)
 {
     typedef typename RT<R>::R4 R4;
@@ -916,7 +1194,16 @@ k_qtraverse(int n, R scaling, R theta2, const typename RT<R>::R4 *__restrict__ p
         if (q.ri.y > 1) {
             const R xd = xi - q.rr.x, yd = yi - q.rr.y;
             const R d2 = xd * xd + yd * yd;
-            if (d2 * theta2 > q.rr.w) {
+            const R lhs = d2 * theta2;
+            bool far = lhs > q.rr.w;
+            if (sizeof(R) == 4 && fabs(lhs - q.rr.w) <= R(DECIDE_BAND) * q.rr.w) {
+                // the host's double region and node, as the CPU decides
+                const double ex = __dsub_rn(px[k], raw[cur].cx), ey = __dsub_rn(py[k], raw[cur].cy);
+                const double sz = raw[cur].size;
+                far = __dmul_rn(__dadd_rn(__dmul_rn(ex, ex), __dmul_rn(ey, ey)), theta2d) >
+                      __dmul_rn(sz, sz);
+            }
+            if (far) {
                 const R g = fdiv(scaling * (mi * q.rr.z), d2);
                 ax += xd * g;
                 ay += yd * g;

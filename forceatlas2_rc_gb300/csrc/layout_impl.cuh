@@ -10,7 +10,8 @@
 //   key, order (+ ping-pong)  u32[n] x 4, counts u32[256 * n / 4096]
 //   psort               R4[n]   (x, y, m, r) in Morton order
 //   child, range        int2[n-1], parent int[2n-1], rope int[n],
-//   visits              int[n-1], agg Agg<R>[n-1], nodes BHNode<R>[n-1]
+//   visits              int[n-1], agg Agg<R>[n-1] (double / float-float sums),
+//                       nodes BHNode<R>[n-1]
 //   packed              R4[n]   (exact repulsion only)
 //   st, status          FP64 speed state, status words
 #pragma once
@@ -66,7 +67,9 @@ template <class R> struct Layout : LayoutBase {
 
     int n = 0, ninc = 0, repulsion = 0, adjust = 0, strong = 0, linlog = 0;
     int any_fixed = 0;
+    int walk = WALK_WARP;
     R scaling = 0, gravity = 0, theta2 = 0;
+    double theta2d = 0.0;
     cudaStream_t s = nullptr;
     DevMem mem;
     R2 *pos = nullptr, *f = nullptr, *fold = nullptr;
@@ -75,6 +78,7 @@ template <class R> struct Layout : LayoutBase {
     int *inc_off = nullptr;
     Inc<R> *inc = nullptr;
     R *bbox = nullptr, *bbox_partial = nullptr;
+    double *quant = nullptr; // min x, min y, Morton scale
     int nbbox = 1, nswing = 1;
     uint32_t *key = nullptr, *order = nullptr;
     SortScratch ss{};
@@ -127,6 +131,7 @@ template <class R> struct Layout : LayoutBase {
         if (want_tree) {
             nbbox = std::min(ceil_div(n, 256), 152 * 4);
             bbox = mem.get<R>(4);
+            quant = mem.get<double>(4);
             bbox_partial = mem.get<R>(4 * (size_t) nbbox);
             key = mem.get<uint32_t>(nn);
             order = mem.get<uint32_t>(nn);
@@ -165,7 +170,8 @@ template <class R> struct Layout : LayoutBase {
             for (int i = 0; i < n && !any_fixed; i++) any_fixed = p->fixed[i] != 0;
         scaling = (R) p->scaling;
         gravity = (R) p->gravity;
-        theta2 = (R) (p->theta * p->theta);
+        theta2d = p->theta * p->theta;
+        theta2 = (R) theta2d;
         FA2_TRY(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking),
                 "could not create a CUDA stream", 1);
         for (auto &e : ev) FA2_TRY(cudaEventCreate(&e), "could not create a CUDA event", 1);
@@ -239,9 +245,9 @@ template <class R> struct Layout : LayoutBase {
     // ---- the steps of one iteration ----
     void launch_build()
     {
-        k_bbox<R><<<nbbox, 256, 0, s>>>(n, pos, bbox_partial, bbox,
+        k_bbox<R><<<nbbox, 256, 0, s>>>(n, pos, bbox_partial, bbox, quant,
                                         (unsigned *) (status + ST_TICKET_BBOX));
-        k_morton<R><<<ceil_div(n, 256), 256, 0, s>>>(n, pos, bbox, key, order);
+        k_morton<R><<<ceil_div(n, 256), 256, 0, s>>>(n, pos, quant, key, order);
     }
     void launch_sort() { sort_pairs(s, n, key, order, ss); }
     void launch_tree()
@@ -255,14 +261,21 @@ template <class R> struct Layout : LayoutBase {
     void launch_repulsion()
     {
         if (repulsion == FA2CU_REPULSION_BH) {
-            if (adjust)
-                k_traverse<R, true><<<ceil_div(n, 256), 256, 0, s>>>(n, scaling, theta2, psort,
-                                                                     nodes, rope, order, f,
-                                                                     status);
-            else
-                k_traverse<R, false><<<ceil_div(n, 256), 256, 0, s>>>(n, scaling, theta2, psort,
-                                                                      nodes, rope, order, f,
-                                                                      status);
+            if (walk == WALK_WARP) {
+                if (adjust)
+                    k_traverse_warp<R, true><<<ceil_div(n, 256), 256, 0, s>>>(
+                        n, scaling, theta2, theta2d, psort, nodes, agg, rope, order, f, status);
+                else
+                    k_traverse_warp<R, false><<<ceil_div(n, 256), 256, 0, s>>>(
+                        n, scaling, theta2, theta2d, psort, nodes, agg, rope, order, f, status);
+            } else {
+                if (adjust)
+                    k_traverse<R, true><<<ceil_div(n, 256), 256, 0, s>>>(
+                        n, scaling, theta2, theta2d, psort, nodes, agg, rope, order, f, status);
+                else
+                    k_traverse<R, false><<<ceil_div(n, 256), 256, 0, s>>>(
+                        n, scaling, theta2, theta2d, psort, nodes, agg, rope, order, f, status);
+            }
         } else {
             k_pack<R><<<ceil_div(n, 256), 256, 0, s>>>(n, adjust, pos, mass, size, packed);
             const int grid = ceil_div(n, FA2_EXACT_THREADS * EXACT_IPT);
@@ -469,6 +482,23 @@ template <class R> struct Layout : LayoutBase {
         return 0;
     }
 
+    int option(const char *name, double value) override
+    {
+        if (!strcmp(name, "walk") && (value == WALK_WARP || value == WALK_THREAD)) {
+            walk = (int) value;
+            cudaSetDevice(device);
+            FA2_TRY(cudaStreamSynchronize(s), "the computation on the GPU failed", 1);
+            if (g1) cudaGraphExecDestroy(g1);
+            if (g8) cudaGraphExecDestroy(g8);
+            g1 = g8 = nullptr;
+            if (capture(&g1, 1)) return 1;
+            if (n <= (1 << 16) && capture(&g8, 8)) return 1;
+            return 0;
+        }
+        set_message("unknown option %s = %g", name, value);
+        return 1;
+    }
+
     int traversal_counts(double out[2]) override
     {
         if (repulsion != FA2CU_REPULSION_BH) {
@@ -480,8 +510,8 @@ template <class R> struct Layout : LayoutBase {
         launch_sort();
         launch_tree();
         cudaMemsetAsync(counts, 0, 2 * sizeof(unsigned long long), s);
-        k_traverse_count<R><<<ceil_div(n, 256), 256, 0, s>>>(n, theta2, psort, nodes, rope,
-                                                             counts);
+        k_traverse_count<R><<<ceil_div(n, 256), 256, 0, s>>>(n, theta2, theta2d, psort, nodes,
+                                                             agg, rope, counts);
         unsigned long long h[2] = {0, 0};
         cudaMemcpyAsync(h, counts, sizeof(h), cudaMemcpyDeviceToHost, s);
         FA2_TRY(cudaStreamSynchronize(s), "the computation on the GPU failed", 1);
@@ -651,13 +681,15 @@ template <class R> struct Repulse : RepulseBase {
         FA2_TRY(cudaStreamSynchronize(s), "the computation on the GPU failed", 1);
         double t1 = now_s();
         t_send += t1 - t0;
-        const R theta2 = (R) (theta * theta);
+        const double theta2d = theta * theta;
+        const R theta2 = (R) theta2d;
+        const double *px = in4, *py = in4 + n; // the host's doubles, tree order
         if (adjust)
-            k_qtraverse<R, true><<<ceil_div(n, 256), 256, 0, s>>>(n, (R) sc, theta2, p, regs,
-                                                                  t->nreg, f, status);
+            k_qtraverse<R, true><<<ceil_div(n, 256), 256, 0, s>>>(
+                n, (R) sc, theta2, theta2d, p, px, py, regs, raw, t->nreg, f, status);
         else
-            k_qtraverse<R, false><<<ceil_div(n, 256), 256, 0, s>>>(n, (R) sc, theta2, p, regs,
-                                                                   t->nreg, f, status);
+            k_qtraverse<R, false><<<ceil_div(n, 256), 256, 0, s>>>(
+                n, (R) sc, theta2, theta2d, p, px, py, regs, raw, t->nreg, f, status);
         FA2_TRY(cudaGetLastError(), "the computation on the GPU failed", 1);
         FA2_TRY(cudaStreamSynchronize(s), "the computation on the GPU failed", 1);
         if (check_status()) return 1;

@@ -25,6 +25,7 @@ struct LayoutBase {
     virtual int tree(const double *pos, uint32_t *key, uint32_t *order, int *child,
                      int *range, int *parent, double *ni) = 0;
     virtual int traversal_counts(double counts[2]) = 0;
+    virtual int option(const char *name, double value) = 0;
     virtual double bytes() const = 0;
     int device = 0;
 };

@@ -256,6 +256,10 @@ class Layout:
         self._check(self.lib.fa2cu_layout_traversal_counts(self.h, dptr(c)))
         return dict(visits=c[0], pairs=c[1])
 
+    def option(self, name: str, value: float):
+        """Tuning option (fa2cu_layout_option), e.g. option("walk", 1)."""
+        self._check(self.lib.fa2cu_layout_option(self.h, name.encode(), float(value)))
+
     @property
     def device_bytes(self) -> float:
         return self.lib.fa2cu_layout_bytes(self.h)

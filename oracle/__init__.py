@@ -89,6 +89,7 @@ def lib():
         for s in ("f", "d"):
             getattr(_lib, f"orc_pipe_forces_{s}").restype = C.c_int
             getattr(_lib, f"orc_pipe_run_{s}").restype = C.c_int
+        _lib.orc_pipe_forces_m.restype = C.c_int
     return _lib
 
 
@@ -346,6 +347,9 @@ def pipe_build(n, pos, mass_, precision="f", which="oracle"):
 
 
 def pipe_forces(p: FullParams, pos, precision="f", which="oracle"):
+    """precision "f" / "d": the reference's float / double construction;
+    "m": the FP32 path of libfa2cuda.so (double construction over the
+    float-rounded inputs, float walk and attraction)."""
     n = p.n
     xy = _pos_cols(pos)
     f = np.zeros(2 * n)

@@ -790,3 +790,129 @@ void orc_pipe_tree(int n, const uint32_t *key, int *child, int *range,
 #include "pipe_impl.h"
 #undef real
 #undef S
+
+/* ------------------------------------------------------------------------ */
+/* The construction of the FP32 path of libfa2cuda.so                       */
+/* ------------------------------------------------------------------------ */
+
+/* The float walk of that path: regions in float, but a region whose test
+ * d^2 theta^2 > size^2 is within 1e-4 of the boundary is decided in double
+ * from the double construction, so that the float path approximates the
+ * regions the double path approximates. */
+static void repulse_mixed(const pipe_ws_f *w, const pipe_ws_d *wd,
+                          float scaling, float theta2, double theta2d,
+                          int adjust, float *f)
+{
+    const int n = w->n;
+    const float *ps = w->psort, *ni = w->ni;
+    for (int k = 0; k < n; k++) {
+        const float xi = ps[4 * k], yi = ps[4 * k + 1];
+        const float mi = ps[4 * k + 2], si = ps[4 * k + 3];
+        float ax = 0.0f, ay = 0.0f;
+        int stack[160];
+        int sp = 0;
+        stack[sp++] = 0;
+        while (sp > 0) {
+            const int r = stack[--sp];
+            int first, last;
+            if (r >= n - 1) {
+                first = last = r - (n - 1);
+            } else {
+                const float xd = xi - ni[4 * r], yd = yi - ni[4 * r + 1];
+                const float d2 = xd * xd + yd * yd;
+                const float lhs = d2 * theta2;
+                int far = lhs > ni[4 * r + 3];
+                if (fabsf(lhs - ni[4 * r + 3]) <= 1e-4f * ni[4 * r + 3]) {
+                    const double ex = (double) xi - wd->ni[4 * r];
+                    const double ey = (double) yi - wd->ni[4 * r + 1];
+                    far = (ex * ex + ey * ey) * theta2d > wd->ni[4 * r + 3];
+                }
+                if (far) {
+                    const float g = scaling * (mi * ni[4 * r + 2]) / d2;
+                    ax += xd * g;
+                    ay += yd * g;
+                    continue;
+                }
+                first = w->range[2 * r];
+                last = w->range[2 * r + 1];
+                if (last - first >= ORC_LEAF) {
+                    stack[sp++] = w->child[2 * r + 1];
+                    stack[sp++] = w->child[2 * r];
+                    continue;
+                }
+            }
+            for (int j = first; j <= last; j++) {
+                if (j == k) continue;
+                const float xd = xi - ps[4 * j], yd = yi - ps[4 * j + 1];
+                const float g = rep_f(xd * xd + yd * yd, mi * ps[4 * j + 2],
+                                      si + ps[4 * j + 3], scaling, adjust);
+                ax += xd * g;
+                ay += yd * g;
+            }
+        }
+        const uint32_t i = w->order[k];
+        f[2 * i] = ax;
+        f[2 * i + 1] = ay;
+    }
+}
+
+/* Forces as that path computes them: the tree is built in double from the
+ * positions and masses rounded to float (keys, order, regions: the double
+ * construction of pipeline.cl), the regions' records are rounded to float,
+ * and the walk (with the decisions above) and the attraction run in float
+ * (pipeline.cl:332-429). */
+int orc_pipe_forces_m(const fa2_full_params *pp, const double *pos,
+                      double *fout)
+{
+    const int n = pp->n;
+    if (n < 2) return 1;
+    pipe_ws_d wd;
+    pipe_ws_f wf;
+    pipe_graph_f gf;
+    memset(&wd, 0, sizeof(wd));
+    memset(&wf, 0, sizeof(wf));
+    memset(&gf, 0, sizeof(gf));
+    double *pr = (double *) malloc(2 * (size_t) n * sizeof(double));
+    double *mr = (double *) malloc((size_t) n * sizeof(double));
+    float *f = (float *) malloc(2 * (size_t) n * sizeof(float));
+    int ok = pr && mr && f && ws_alloc_d(&wd, n) && ws_alloc_f(&wf, n) &&
+             graph_load_f(&gf, pp, pos);
+    if (ok) {
+        for (int i = 0; i < n; i++) {
+            pr[2 * i] = (double) gf.p[2 * i];
+            pr[2 * i + 1] = (double) gf.p[2 * i + 1];
+            mr[i] = (double) gf.mass[i];
+        }
+        build_core_d(&wd, pr, mr, NULL, 0);
+        memcpy(wf.key, wd.key, (size_t) n * 4);
+        memcpy(wf.order, wd.order, (size_t) n * 4);
+        memcpy(wf.child, wd.child, 2 * (size_t) (n - 1) * sizeof(int));
+        memcpy(wf.range, wd.range, 2 * (size_t) (n - 1) * sizeof(int));
+        for (size_t r = 0; r < 4 * (size_t) (n - 1); r++)
+            wf.ni[r] = (float) wd.ni[r];
+        for (int k = 0; k < n; k++) {
+            const uint32_t i = wf.order[k];
+            wf.psort[4 * k] = gf.p[2 * i];
+            wf.psort[4 * k + 1] = gf.p[2 * i + 1];
+            wf.psort[4 * k + 2] = gf.mass[i];
+            wf.psort[4 * k + 3] = pp->adjust ? gf.size[i] : 0.0f;
+        }
+        repulse_mixed(&wf, &wd, (float) pp->scaling,
+                      (float) (pp->theta * pp->theta), pp->theta * pp->theta,
+                      pp->adjust, f);
+        attract_core_f(n, (float) pp->gravity, pp->strong, pp->linlog,
+                       pp->adjust, gf.p, gf.mass, gf.size, pp->inc_off,
+                       pp->inc_node, gf.coef, f);
+        for (int i = 0; i < n; i++) {
+            fout[i] = (double) f[2 * i];
+            fout[n + i] = (double) f[2 * i + 1];
+        }
+    }
+    ws_free_d(&wd);
+    ws_free_f(&wf);
+    graph_free_f(&gf);
+    free(pr);
+    free(mr);
+    free(f);
+    return ok ? 0 : 1;
+}

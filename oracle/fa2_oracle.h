@@ -135,6 +135,12 @@ void orc_pipe_tree(int n, const uint32_t *key, int *child, int *range,
 ORC_PIPE_DECLARE(float, f)
 ORC_PIPE_DECLARE(double, d)
 
+/* Forces of the FP32 path of libfa2cuda.so: tree of the double construction
+ * over the float-rounded positions and masses, walk and attraction in float
+ * (pipeline.cl:332-429). */
+int orc_pipe_forces_m(const fa2_full_params *p, const double *pos,
+                      double *f);
+
 #ifdef __cplusplus
 }
 #endif

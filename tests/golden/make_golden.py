@@ -113,6 +113,13 @@ def main():
     out.update(pb_pos=p2, pb_mass=m2, pb_from=a2, pb_to=b2)
     line = np.stack([np.arange(64, dtype=float), np.zeros(64)], axis=1)
     two = np.array([[0.0, 0.0], [1.0, 1.0]])
+    # the FP32 path builds the double construction over float-rounded
+    # positions
+    p32 = p2.astype(np.float32).astype(np.float64)
+    out["pb32_pos"] = p32
+    r = O.pipe_build(n2, p32, m2, "d", which="ref")
+    for k, v in r.items():
+        out[f"pb32_d_{k}"] = v
     for prec in "fd":
         r = O.pipe_build(n2, p2, m2, prec, which="ref")
         for k, v in r.items():
