@@ -367,10 +367,12 @@ def main():
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu:
         threads = os.cpu_count() or 1
-        cv, cdt = cpu_sample(n, a, b, 3, threads)
+        iters = 40 if not args.small else 10
+        cv, cdt = cpu_sample(n, a, b, iters, threads)
         cpu = {"value": cv, "unit": UNIT, "cores": threads, "kind": "port",
-               "sample": f"3 iterations of the full {n}-node workload (after 1 "
-                         f"warm-up), C_forceatlas2 quadtree engine, {cdt:.1f} s"}
+               "sample": f"{iters} iterations of the full {n}-node workload "
+                         f"(after 1 warm-up), C_forceatlas2 quadtree engine, "
+                         f"{cdt:.1f} s"}
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws,
