@@ -204,7 +204,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--profile-only", action="store_true",
                     help="warm-up and a few iterations only (for ncu)")
-    ap.add_argument("--walk", default="warp", choices=["warp", "thread"],
+    ap.add_argument("--walk", default="thread", choices=["warp", "thread", "wide"],
                     help="Barnes-Hut walk (identical forces)")
     args = ap.parse_args()
     if args.impl == "reference":
@@ -229,8 +229,8 @@ def main():
     g = Graph(n, a, b, np.ones(len(a)), outbound=True)
     kw = dict(scaling=2.0, gravity=1.0, theta=1.2, linlog=True, device=local)
     L = Layout(g, pos, precision="single", repulsion=REPULSION_BH, **kw)
-    if args.walk == "thread":
-        L.option("walk", 1)
+    if args.walk != "thread":
+        L.option("walk", {"warp": 0, "wide": 2}[args.walk])
     stream = torch.cuda.ExternalStream(L.stream, device=local)
 
     if args.profile_only:
@@ -356,7 +356,9 @@ def main():
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"],
                 "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"],
                 "traffic": None,
-                "kernel": "k_traverse_warp<float>" if args.walk == "warp" else "k_traverse<float>",
+                "kernel": {"warp": "k_traverse_warp<float>",
+                           "thread": "k_traverse<float, 6>",
+                           "wide": "k_traverse<float, 1>"}[args.walk],
                 "peak_kind": f"{kind} (HBM copy)",
                 "launch_ms": ph["repulsion"],
                 "l2_request_bytes": l2_bytes,

@@ -23,8 +23,10 @@ void set_cuda_error(const char *what, cudaError_t e);
         }                                                                      \
     } while (0)
 
-// Barnes-Hut walk variants (both give identical forces).
-enum { WALK_WARP = 0, WALK_THREAD = 1 };
+// Barnes-Hut walk variants (all give identical forces): warp-synchronous;
+// one walk per thread at 6 blocks of 256 per SM (<= 40 registers); one walk
+// per thread with the registers the compiler wants.
+enum { WALK_WARP = 0, WALK_THREAD = 1, WALK_THREAD_WIDE = 2 };
 
 // Device-side status words (one int each in a session's `status` buffer).
 enum {

@@ -414,9 +414,14 @@ k_aggregate(int n, const typename RT<R>::R4 *__restrict__ psort,
             atomicOr(status + ST_ERROR, ERR_BOUNDS);
             return;
         }
-        __threadfence();
-        if (atomicAdd(&visits[r], 1) == 0) return;
-        __threadfence();
+        // release: this thread's region (or leaf) is written before it
+        // arrives; acquire: the sibling's is visible to the second arrival
+        int prior;
+        asm volatile("atom.add.acq_rel.gpu.s32 %0, [%1], 1;"
+                     : "=r"(prior)
+                     : "l"(visits + r)
+                     : "memory");
+        if (prior == 0) return;
         const int2 c = child[r];
         if (c.x < 0 || c.y < 0 || c.x >= nl + n || c.y >= nl + n) {
             atomicOr(status + ST_ERROR, ERR_BOUNDS);
@@ -450,8 +455,19 @@ k_aggregate(int n, const typename RT<R>::R4 *__restrict__ psort,
 // approximation error itself, ~1e-2 of that region's pull).
 constexpr float DECIDE_BAND = 1e-4f;
 
-template <class R, bool ADJUST>
-__global__ void __launch_bounds__(256)
+// The rare re-decision in double, out of line so that its registers do not
+// weigh on the walk.
+template <class R>
+__device__ __noinline__ bool far_fp64_nl(const Agg<R> *q, double xi, double yi, double theta2d)
+{
+    return far_fp64(*q, xi, yi, theta2d);
+}
+
+__device__ __forceinline__ float fabs_r(float a) { return fabsf(a); }
+__device__ __forceinline__ double fabs_r(double a) { return fabs(a); }
+
+template <class R, bool ADJUST, int MINB>
+__global__ void __launch_bounds__(256, MINB)
 k_traverse(int n, R scaling, R theta2, double theta2d,
            const typename RT<R>::R4 *__restrict__ psort,
            const BHNode<R> *__restrict__ nodes, const Agg<R> *__restrict__ agg,
@@ -470,46 +486,51 @@ k_traverse(int n, R scaling, R theta2, double theta2d,
     // once: more steps than that, or an index out of range, is a bug
     const int cap = 4 * n + 64;
     for (int step = 0;; step++) {
+        if (j > jend) { // no pending node pair: the next region
+            if (cur < 0) break;
+            if (cur >= nl) { // a single node: a pair, computed in this step
+                j = jend = cur - nl;
+                cur = rope[j];
+            }
+        }
         if (step > cap || cur >= nl + n || jend >= n) {
             atomicOr(status + ST_ERROR, ERR_BOUNDS);
             break;
         }
-        if (j <= jend) {
-            if (j != k) {
-                const R4 q = psort[j];
-                const R xd = xi - q.x, yd = yi - q.y;
-                const R g = rep_factor<R, ADJUST>(xd * xd + yd * yd, mi * q.z,
-                                                  si + q.w, scaling);
-                ax += xd * g;
-                ay += yd * g;
-            }
-            ++j;
-            continue;
-        }
-        if (cur < 0) break;
-        if (cur >= nl) { // a single node
-            j = jend = cur - nl;
-            cur = rope[j];
-            continue;
-        }
-        const BHNode<R> nd = nodes[cur];
-        const R xd = xi - nd.c.x, yd = yi - nd.c.y;
+        // one 16-byte record per step, for a pair (x, y, m, r) as for a
+        // region (cx, cy, m, size^2): the force has the same form
+        const bool pair = j <= jend;
+        const R4 q = pair ? psort[j] : nodes[cur].c;
+        const R xd = xi - q.x, yd = yi - q.y;
         const R d2 = xd * xd + yd * yd;
-        const R lhs = d2 * theta2;
-        bool far = lhs > nd.c.w;
-        if (sizeof(R) == 4 && fabs(lhs - nd.c.w) <= R(DECIDE_BAND) * nd.c.w)
-            far = far_fp64(agg[cur], (double) xi, (double) yi, theta2d);
-        if (far) {
-            const R g = fdiv(scaling * (mi * nd.c.z), d2);
+        bool take;
+        if (pair) {
+            take = j != k;
+            ++j;
+        } else {
+            const int4 t = nodes[cur].t;
+            const R lhs = d2 * theta2;
+            take = lhs > q.w;
+            if (sizeof(R) == 4 && fabs_r(lhs - q.w) <= R(DECIDE_BAND) * q.w)
+                take = far_fp64(agg[cur], (double) xi, (double) yi, theta2d);
+            if (take) {
+                cur = t.y;
+            } else if (t.w - t.z >= 8) {
+                cur = t.x;
+            } else {
+                j = t.z;
+                jend = t.w;
+                cur = t.y;
+            }
+        }
+        if (take) {
+            // region: scaling * (mi * m) / d2 with d2 > 0 (pipeline.cl:357-361);
+            // pair: the factor of pipeline.cl:46-55, the same expression
+            // when the radii are not used
+            const R g = (ADJUST && pair) ? rep_factor<R, true>(d2, mi * q.z, si + q.w, scaling)
+                                         : rep_factor<R, false>(d2, mi * q.z, R(0), scaling);
             ax += xd * g;
             ay += yd * g;
-            cur = nd.t.y;
-        } else if (nd.t.w - nd.t.z >= 8) {
-            cur = nd.t.x;
-        } else {
-            j = nd.t.z;
-            jend = nd.t.w;
-            cur = nd.t.y;
         }
     }
     f[order[k]] = mk2<R>(ax, ay);
@@ -570,7 +591,7 @@ k_traverse_warp(int n, R scaling, R theta2, double theta2d,
             const R d2 = xd * xd + yd * yd;
             const R lhs = d2 * theta2;
             bool far = lhs > nd.c.w;
-            if (sizeof(R) == 4 && fabs(lhs - nd.c.w) <= R(DECIDE_BAND) * nd.c.w)
+            if (sizeof(R) == 4 && fabs_r(lhs - nd.c.w) <= R(DECIDE_BAND) * nd.c.w)
                 far = far_fp64(agg[cur], (double) xi, (double) yi, theta2d);
             if (far) {
                 const R g = fdiv(scaling * (mi * nd.c.z), d2);
@@ -627,7 +648,7 @@ k_traverse_count(int n, R theta2, double theta2d, const typename RT<R>::R4 *__re
             const R d2 = xd * xd + yd * yd;
             const R lhs = d2 * theta2;
             bool far = lhs > nd.c.w;
-            if (sizeof(R) == 4 && fabs(lhs - nd.c.w) <= R(DECIDE_BAND) * nd.c.w)
+            if (sizeof(R) == 4 && fabs_r(lhs - nd.c.w) <= R(DECIDE_BAND) * nd.c.w)
                 far = far_fp64(agg[cur], (double) me.x, (double) me.y, theta2d);
             if (far) {
                 cur = nd.t.y;
@@ -1196,7 +1217,7 @@ k_qtraverse(int n, R scaling, R theta2, double theta2d, const typename RT<R>::R4
             const R d2 = xd * xd + yd * yd;
             const R lhs = d2 * theta2;
             bool far = lhs > q.rr.w;
-            if (sizeof(R) == 4 && fabs(lhs - q.rr.w) <= R(DECIDE_BAND) * q.rr.w) {
+            if (sizeof(R) == 4 && fabs_r(lhs - q.rr.w) <= R(DECIDE_BAND) * q.rr.w) {
                 // the host's double region and node, as the CPU decides
                 const double ex = __dsub_rn(px[k], raw[cur].cx), ey = __dsub_rn(py[k], raw[cur].cy);
                 const double sz = raw[cur].size;

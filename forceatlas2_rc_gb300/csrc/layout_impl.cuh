@@ -67,7 +67,7 @@ template <class R> struct Layout : LayoutBase {
 
     int n = 0, ninc = 0, repulsion = 0, adjust = 0, strong = 0, linlog = 0;
     int any_fixed = 0;
-    int walk = WALK_WARP;
+    int walk = WALK_THREAD;
     R scaling = 0, gravity = 0, theta2 = 0;
     double theta2d = 0.0;
     cudaStream_t s = nullptr;
@@ -268,12 +268,19 @@ template <class R> struct Layout : LayoutBase {
                 else
                     k_traverse_warp<R, false><<<ceil_div(n, 256), 256, 0, s>>>(
                         n, scaling, theta2, theta2d, psort, nodes, agg, rope, order, f, status);
-            } else {
+            } else if (walk == WALK_THREAD) {
                 if (adjust)
-                    k_traverse<R, true><<<ceil_div(n, 256), 256, 0, s>>>(
+                    k_traverse<R, true, 6><<<ceil_div(n, 256), 256, 0, s>>>(
                         n, scaling, theta2, theta2d, psort, nodes, agg, rope, order, f, status);
                 else
-                    k_traverse<R, false><<<ceil_div(n, 256), 256, 0, s>>>(
+                    k_traverse<R, false, 6><<<ceil_div(n, 256), 256, 0, s>>>(
+                        n, scaling, theta2, theta2d, psort, nodes, agg, rope, order, f, status);
+            } else {
+                if (adjust)
+                    k_traverse<R, true, 1><<<ceil_div(n, 256), 256, 0, s>>>(
+                        n, scaling, theta2, theta2d, psort, nodes, agg, rope, order, f, status);
+                else
+                    k_traverse<R, false, 1><<<ceil_div(n, 256), 256, 0, s>>>(
                         n, scaling, theta2, theta2d, psort, nodes, agg, rope, order, f, status);
             }
         } else {
@@ -484,7 +491,8 @@ template <class R> struct Layout : LayoutBase {
 
     int option(const char *name, double value) override
     {
-        if (!strcmp(name, "walk") && (value == WALK_WARP || value == WALK_THREAD)) {
+        if (!strcmp(name, "walk") &&
+            (value == WALK_WARP || value == WALK_THREAD || value == WALK_THREAD_WIDE)) {
             walk = (int) value;
             cudaSetDevice(device);
             FA2_TRY(cudaStreamSynchronize(s), "the computation on the GPU failed", 1);

@@ -75,9 +75,10 @@ int fa2cu_layout_tree(fa2cu_layout *L, const double *pos, uint32_t *key,
  * the current positions (an instrumented, untimed variant). */
 int fa2cu_layout_traversal_counts(fa2cu_layout *L, double counts[2]);
 
-/* Set a tuning option of the layout: "walk" = 0 for the warp-synchronous
- * Barnes-Hut walk (default), 1 for one independent walk per thread. Both
- * give identical forces. */
+/* Set a tuning option of the layout: "walk" = 1 for one independent
+ * Barnes-Hut walk per thread (default), 0 for the warp-synchronous walk
+ * (lanes walk together, keeping their own decisions). Both give identical
+ * forces. */
 int fa2cu_layout_option(fa2cu_layout *L, const char *name, double value);
 
 /* Bytes of device memory held by the layout. */

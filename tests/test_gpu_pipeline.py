@@ -260,11 +260,17 @@ def test_warp_walk_equals_thread_walk(gpu, prec, adjust):
     size = f32(np.random.default_rng(3).uniform(0.5, 4.0, n))
     with make_layout(n, a, b, w, pos, prec, size=size, adjust=adjust,
                      theta=1.2) as L:
-        fw = L.forces(pos)
-        L.option("walk", 1)
         ft = L.forces(pos)
         L.option("walk", 0)
+        fw = L.forces(pos)
+        L.option("walk", 1)
+        ft2 = L.forces(pos)
+        L.option("walk", 0)
         fw2 = L.forces(pos)
+        L.option("walk", 2)
+        fwide = L.forces(pos)
+    np.testing.assert_array_equal(ft, ft2)
+    np.testing.assert_array_equal(ft, fwide)
     np.testing.assert_array_equal(fw, fw2)
     if prec == "double":
         np.testing.assert_array_equal(fw, ft)
