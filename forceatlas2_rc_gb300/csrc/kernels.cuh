@@ -373,6 +373,22 @@ __device__ __forceinline__ float4 agg_record(const Agg<float> &q)
                        2.0f * (w * w + h * h));
 }
 
+// The double construction's (cx, cy, size^2) of an FP32-path region, from its
+// float-float sums (the walk's rare re-decisions read it).
+__device__ __forceinline__ double4_32a agg_record_dd(const Agg<float> &q)
+{
+    const double m = ff_to_double(q.m);
+    const double w = __dsub_rn((double) q.maxx, (double) q.minx);
+    const double h = __dsub_rn((double) q.maxy, (double) q.miny);
+    double4_32a c;
+    c.x = __ddiv_rn(ff_to_double(q.mx), m);
+    c.y = __ddiv_rn(ff_to_double(q.my), m);
+    c.z = __dmul_rn(2.0, __dadd_rn(__dmul_rn(w, w), __dmul_rn(h, h)));
+    c.w = 0.0;
+    return c;
+}
+__device__ __forceinline__ double4_32a agg_record_dd(const Agg<double> &q) { return agg_record(q); }
+
 // The opening test of the double construction, for a region of either path.
 __device__ __forceinline__ bool far_fp64(const Agg<double> &q, double xi, double yi,
                                          double theta2d)
@@ -402,7 +418,8 @@ k_aggregate(int n, const typename RT<R>::R4 *__restrict__ psort,
             const int2 *__restrict__ child, const int *__restrict__ parent,
             const int2 *__restrict__ range, const int *__restrict__ rope,
             int *__restrict__ visits, Agg<R> *__restrict__ agg,
-            BHNode<R> *__restrict__ nodes, int *__restrict__ status)
+            BHNode<R> *__restrict__ nodes, double4_32a *__restrict__ dn,
+            int *__restrict__ status)
 {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
@@ -436,6 +453,7 @@ k_aggregate(int n, const typename RT<R>::R4 *__restrict__ psort,
         nd.c = agg_record(q);
         nd.t = make_int4(c.x, rope[rg.y], rg.x, rg.y);
         nodes[r] = nd;
+        if (dn) dn[r] = agg_record_dd(q);
         r = parent[r];
     }
 }
@@ -455,22 +473,25 @@ k_aggregate(int n, const typename RT<R>::R4 *__restrict__ psort,
 // approximation error itself, ~1e-2 of that region's pull).
 constexpr float DECIDE_BAND = 1e-4f;
 
-// The rare re-decision in double, out of line so that its registers do not
-// weigh on the walk.
-template <class R>
-__device__ __noinline__ bool far_fp64_nl(const Agg<R> *q, double xi, double yi, double theta2d)
-{
-    return far_fp64(*q, xi, yi, theta2d);
-}
-
 __device__ __forceinline__ float fabs_r(float a) { return fabsf(a); }
 __device__ __forceinline__ double fabs_r(double a) { return fabs(a); }
+
+// The opening test of the double construction from a region's precomputed
+// double record (cx, cy, size^2): the rare re-decision of the FP32 walk.
+__device__ __forceinline__ bool far_dd(const double4_32a *dn, int r, float xi, float yi,
+                                       double theta2d)
+{
+    const double2 c = *reinterpret_cast<const double2 *>(dn + r);
+    const double s2 = dn[r].z;
+    const double xd = __dsub_rn((double) xi, c.x), yd = __dsub_rn((double) yi, c.y);
+    return __dmul_rn(__dadd_rn(__dmul_rn(xd, xd), __dmul_rn(yd, yd)), theta2d) > s2;
+}
 
 template <class R, bool ADJUST, int MINB>
 __global__ void __launch_bounds__(256, MINB)
 k_traverse(int n, R scaling, R theta2, double theta2d,
            const typename RT<R>::R4 *__restrict__ psort,
-           const BHNode<R> *__restrict__ nodes, const Agg<R> *__restrict__ agg,
+           const BHNode<R> *__restrict__ nodes, const double4_32a *__restrict__ dn,
            const int *__restrict__ rope, const uint32_t *__restrict__ order,
            typename RT<R>::R2 *__restrict__ f, int *__restrict__ status)
 {
@@ -486,51 +507,46 @@ k_traverse(int n, R scaling, R theta2, double theta2d,
     // once: more steps than that, or an index out of range, is a bug
     const int cap = 4 * n + 64;
     for (int step = 0;; step++) {
-        if (j > jend) { // no pending node pair: the next region
-            if (cur < 0) break;
-            if (cur >= nl) { // a single node: a pair, computed in this step
-                j = jend = cur - nl;
-                cur = rope[j];
-            }
-        }
         if (step > cap || cur >= nl + n || jend >= n) {
             atomicOr(status + ST_ERROR, ERR_BOUNDS);
             break;
         }
-        // one 16-byte record per step, for a pair (x, y, m, r) as for a
-        // region (cx, cy, m, size^2): the force has the same form
-        const bool pair = j <= jend;
-        const R4 q = pair ? psort[j] : nodes[cur].c;
-        const R xd = xi - q.x, yd = yi - q.y;
-        const R d2 = xd * xd + yd * yd;
-        bool take;
-        if (pair) {
-            take = j != k;
-            ++j;
-        } else {
-            const int4 t = nodes[cur].t;
-            const R lhs = d2 * theta2;
-            take = lhs > q.w;
-            if (sizeof(R) == 4 && fabs_r(lhs - q.w) <= R(DECIDE_BAND) * q.w)
-                take = far_fp64(agg[cur], (double) xi, (double) yi, theta2d);
-            if (take) {
-                cur = t.y;
-            } else if (t.w - t.z >= 8) {
-                cur = t.x;
-            } else {
-                j = t.z;
-                jend = t.w;
-                cur = t.y;
+        if (j <= jend) {
+            if (j != k) {
+                const R4 q = psort[j];
+                const R xd = xi - q.x, yd = yi - q.y;
+                const R g = rep_factor<R, ADJUST>(xd * xd + yd * yd, mi * q.z,
+                                                  si + q.w, scaling);
+                ax += xd * g;
+                ay += yd * g;
             }
+            ++j;
+            continue;
         }
-        if (take) {
-            // region: scaling * (mi * m) / d2 with d2 > 0 (pipeline.cl:357-361);
-            // pair: the factor of pipeline.cl:46-55, the same expression
-            // when the radii are not used
-            const R g = (ADJUST && pair) ? rep_factor<R, true>(d2, mi * q.z, si + q.w, scaling)
-                                         : rep_factor<R, false>(d2, mi * q.z, R(0), scaling);
+        if (cur < 0) break;
+        if (cur >= nl) { // a single node
+            j = jend = cur - nl;
+            cur = rope[j];
+            continue;
+        }
+        const BHNode<R> nd = nodes[cur];
+        const R xd = xi - nd.c.x, yd = yi - nd.c.y;
+        const R d2 = xd * xd + yd * yd;
+        const R lhs = d2 * theta2;
+        bool far = lhs > nd.c.w;
+        if (sizeof(R) == 4 && fabs_r(lhs - nd.c.w) <= R(DECIDE_BAND) * nd.c.w)
+            far = far_dd(dn, cur, (float) xi, (float) yi, theta2d);
+        if (far) {
+            const R g = fdiv(scaling * (mi * nd.c.z), d2);
             ax += xd * g;
             ay += yd * g;
+            cur = nd.t.y;
+        } else if (nd.t.w - nd.t.z >= 8) {
+            cur = nd.t.x;
+        } else {
+            j = nd.t.z;
+            jend = nd.t.w;
+            cur = nd.t.y;
         }
     }
     f[order[k]] = mk2<R>(ax, ay);
@@ -549,7 +565,7 @@ template <class R, bool ADJUST>
 __global__ void __launch_bounds__(256)
 k_traverse_warp(int n, R scaling, R theta2, double theta2d,
                 const typename RT<R>::R4 *__restrict__ psort,
-                const BHNode<R> *__restrict__ nodes, const Agg<R> *__restrict__ agg,
+                const BHNode<R> *__restrict__ nodes, const double4_32a *__restrict__ dn,
                 const int *__restrict__ rope, const uint32_t *__restrict__ order,
                 typename RT<R>::R2 *__restrict__ f, int *__restrict__ status)
 {
@@ -592,7 +608,7 @@ k_traverse_warp(int n, R scaling, R theta2, double theta2d,
             const R lhs = d2 * theta2;
             bool far = lhs > nd.c.w;
             if (sizeof(R) == 4 && fabs_r(lhs - nd.c.w) <= R(DECIDE_BAND) * nd.c.w)
-                far = far_fp64(agg[cur], (double) xi, (double) yi, theta2d);
+                far = far_dd(dn, cur, (float) xi, (float) yi, theta2d);
             if (far) {
                 const R g = fdiv(scaling * (mi * nd.c.z), d2);
                 ax += xd * g;
@@ -627,7 +643,7 @@ k_traverse_warp(int n, R scaling, R theta2, double theta2d,
 template <class R>
 __global__ void __launch_bounds__(256)
 k_traverse_count(int n, R theta2, double theta2d, const typename RT<R>::R4 *__restrict__ psort,
-                 const BHNode<R> *__restrict__ nodes, const Agg<R> *__restrict__ agg,
+                 const BHNode<R> *__restrict__ nodes, const double4_32a *__restrict__ dn,
                  const int *__restrict__ rope, unsigned long long *__restrict__ counts)
 {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -649,7 +665,7 @@ k_traverse_count(int n, R theta2, double theta2d, const typename RT<R>::R4 *__re
             const R lhs = d2 * theta2;
             bool far = lhs > nd.c.w;
             if (sizeof(R) == 4 && fabs_r(lhs - nd.c.w) <= R(DECIDE_BAND) * nd.c.w)
-                far = far_fp64(agg[cur], (double) me.x, (double) me.y, theta2d);
+                far = far_dd(dn, cur, (float) me.x, (float) me.y, theta2d);
             if (far) {
                 cur = nd.t.y;
             } else if (nd.t.w - nd.t.z >= 8) {
