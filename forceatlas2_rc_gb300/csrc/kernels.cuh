@@ -373,53 +373,13 @@ __device__ __forceinline__ float4 agg_record(const Agg<float> &q)
                        2.0f * (w * w + h * h));
 }
 
-// The double construction's (cx, cy, size^2) of an FP32-path region, from its
-// float-float sums (the walk's rare re-decisions read it).
-__device__ __forceinline__ double4_32a agg_record_dd(const Agg<float> &q)
-{
-    const double m = ff_to_double(q.m);
-    const double w = __dsub_rn((double) q.maxx, (double) q.minx);
-    const double h = __dsub_rn((double) q.maxy, (double) q.miny);
-    double4_32a c;
-    c.x = __ddiv_rn(ff_to_double(q.mx), m);
-    c.y = __ddiv_rn(ff_to_double(q.my), m);
-    c.z = __dmul_rn(2.0, __dadd_rn(__dmul_rn(w, w), __dmul_rn(h, h)));
-    c.w = 0.0;
-    return c;
-}
-__device__ __forceinline__ double4_32a agg_record_dd(const Agg<double> &q) { return agg_record(q); }
-
-// The opening test of the double construction, for a region of either path.
-__device__ __forceinline__ bool far_fp64(const Agg<double> &q, double xi, double yi,
-                                         double theta2d)
-{
-    const double4_32a c = agg_record(q);
-    const double xd = __dsub_rn(xi, c.x), yd = __dsub_rn(yi, c.y);
-    const double d2 = __dadd_rn(__dmul_rn(xd, xd), __dmul_rn(yd, yd));
-    return __dmul_rn(d2, theta2d) > c.w;
-}
-
-__device__ __forceinline__ bool far_fp64(const Agg<float> &q, double xi, double yi,
-                                         double theta2d)
-{
-    const double m = ff_to_double(q.m);
-    const double cx = __ddiv_rn(ff_to_double(q.mx), m), cy = __ddiv_rn(ff_to_double(q.my), m);
-    const double w = __dsub_rn((double) q.maxx, (double) q.minx);
-    const double h = __dsub_rn((double) q.maxy, (double) q.miny);
-    const double s2 = __dmul_rn(2.0, __dadd_rn(__dmul_rn(w, w), __dmul_rn(h, h)));
-    const double xd = __dsub_rn(xi, cx), yd = __dsub_rn(yi, cy);
-    const double d2 = __dadd_rn(__dmul_rn(xd, xd), __dmul_rn(yd, yd));
-    return __dmul_rn(d2, theta2d) > s2;
-}
-
 template <class R>
 __global__ void __launch_bounds__(256)
 k_aggregate(int n, const typename RT<R>::R4 *__restrict__ psort,
             const int2 *__restrict__ child, const int *__restrict__ parent,
             const int2 *__restrict__ range, const int *__restrict__ rope,
             int *__restrict__ visits, Agg<R> *__restrict__ agg,
-            BHNode<R> *__restrict__ nodes, double4_32a *__restrict__ dn,
-            int *__restrict__ status)
+            BHNode<R> *__restrict__ nodes, int *__restrict__ status)
 {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
@@ -453,7 +413,6 @@ k_aggregate(int n, const typename RT<R>::R4 *__restrict__ psort,
         nd.c = agg_record(q);
         nd.t = make_int4(c.x, rope[rg.y], rg.x, rg.y);
         nodes[r] = nd;
-        if (dn) dn[r] = agg_record_dd(q);
         r = parent[r];
     }
 }
@@ -476,22 +435,33 @@ constexpr float DECIDE_BAND = 1e-4f;
 __device__ __forceinline__ float fabs_r(float a) { return fabsf(a); }
 __device__ __forceinline__ double fabs_r(double a) { return fabs(a); }
 
-// The opening test of the double construction from a region's precomputed
-// double record (cx, cy, size^2): the rare re-decision of the FP32 walk.
-__device__ __forceinline__ bool far_dd(const double4_32a *dn, int r, float xi, float yi,
-                                       double theta2d)
+// The rare re-decision of the FP32 walk, in double, from a region's
+// float-float sums and float bounding box (exact in double): without
+// dividing, d^2 theta^2 > size^2 is (m x - sum m x)^2 + (m y - sum m y)^2
+// times theta^2 > size^2 m^2. It agrees with the double construction's test
+// except within ~1e-14 of the boundary.
+__device__ __forceinline__ bool far_dd(const Agg<float> *a, float xi, float yi, double theta2d)
 {
-    const double2 c = *reinterpret_cast<const double2 *>(dn + r);
-    const double s2 = dn[r].z;
-    const double xd = __dsub_rn((double) xi, c.x), yd = __dsub_rn((double) yi, c.y);
-    return __dmul_rn(__dadd_rn(__dmul_rn(xd, xd), __dmul_rn(yd, yd)), theta2d) > s2;
+    const float4 *p = reinterpret_cast<const float4 *>(a);
+    const float4 box = p[0], q1 = p[1], q2 = p[2];
+    const double m = (double) q1.x + (double) q1.y;
+    const double mx = (double) q1.z + (double) q1.w;
+    const double my = (double) q2.x + (double) q2.y;
+    const double w = (double) box.z - (double) box.x, h = (double) box.w - (double) box.y;
+    const double s2 = 2.0 * (w * w + h * h);
+    const double X = m * (double) xi - mx, Y = m * (double) yi - my;
+    return (X * X + Y * Y) * theta2d > s2 * (m * m);
+}
+__device__ __forceinline__ bool far_dd(const Agg<double> *a, float xi, float yi, double theta2d)
+{
+    return false; // the FP64 walk decides in double directly
 }
 
 template <class R, bool ADJUST, int MINB>
 __global__ void __launch_bounds__(256, MINB)
 k_traverse(int n, R scaling, R theta2, double theta2d,
            const typename RT<R>::R4 *__restrict__ psort,
-           const BHNode<R> *__restrict__ nodes, const double4_32a *__restrict__ dn,
+           const BHNode<R> *__restrict__ nodes, const Agg<R> *__restrict__ agg,
            const int *__restrict__ rope, const uint32_t *__restrict__ order,
            typename RT<R>::R2 *__restrict__ f, int *__restrict__ status)
 {
@@ -535,7 +505,7 @@ k_traverse(int n, R scaling, R theta2, double theta2d,
         const R lhs = d2 * theta2;
         bool far = lhs > nd.c.w;
         if (sizeof(R) == 4 && fabs_r(lhs - nd.c.w) <= R(DECIDE_BAND) * nd.c.w)
-            far = far_dd(dn, cur, (float) xi, (float) yi, theta2d);
+            far = far_dd(agg + cur, (float) xi, (float) yi, theta2d);
         if (far) {
             const R g = fdiv(scaling * (mi * nd.c.z), d2);
             ax += xd * g;
@@ -565,7 +535,7 @@ template <class R, bool ADJUST>
 __global__ void __launch_bounds__(256)
 k_traverse_warp(int n, R scaling, R theta2, double theta2d,
                 const typename RT<R>::R4 *__restrict__ psort,
-                const BHNode<R> *__restrict__ nodes, const double4_32a *__restrict__ dn,
+                const BHNode<R> *__restrict__ nodes, const Agg<R> *__restrict__ agg,
                 const int *__restrict__ rope, const uint32_t *__restrict__ order,
                 typename RT<R>::R2 *__restrict__ f, int *__restrict__ status)
 {
@@ -608,7 +578,7 @@ k_traverse_warp(int n, R scaling, R theta2, double theta2d,
             const R lhs = d2 * theta2;
             bool far = lhs > nd.c.w;
             if (sizeof(R) == 4 && fabs_r(lhs - nd.c.w) <= R(DECIDE_BAND) * nd.c.w)
-                far = far_dd(dn, cur, (float) xi, (float) yi, theta2d);
+                far = far_dd(agg + cur, (float) xi, (float) yi, theta2d);
             if (far) {
                 const R g = fdiv(scaling * (mi * nd.c.z), d2);
                 ax += xd * g;
@@ -643,7 +613,7 @@ k_traverse_warp(int n, R scaling, R theta2, double theta2d,
 template <class R>
 __global__ void __launch_bounds__(256)
 k_traverse_count(int n, R theta2, double theta2d, const typename RT<R>::R4 *__restrict__ psort,
-                 const BHNode<R> *__restrict__ nodes, const double4_32a *__restrict__ dn,
+                 const BHNode<R> *__restrict__ nodes, const Agg<R> *__restrict__ agg,
                  const int *__restrict__ rope, unsigned long long *__restrict__ counts)
 {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -665,7 +635,7 @@ k_traverse_count(int n, R theta2, double theta2d, const typename RT<R>::R4 *__re
             const R lhs = d2 * theta2;
             bool far = lhs > nd.c.w;
             if (sizeof(R) == 4 && fabs_r(lhs - nd.c.w) <= R(DECIDE_BAND) * nd.c.w)
-                far = far_dd(dn, cur, (float) me.x, (float) me.y, theta2d);
+                far = far_dd(agg + cur, (float) me.x, (float) me.y, theta2d);
             if (far) {
                 cur = nd.t.y;
             } else if (nd.t.w - nd.t.z >= 8) {

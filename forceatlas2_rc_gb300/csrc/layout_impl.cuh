@@ -87,7 +87,6 @@ template <class R> struct Layout : LayoutBase {
     int *parent = nullptr, *rope = nullptr, *visits = nullptr;
     Agg<R> *agg = nullptr;
     BHNode<R> *nodes = nullptr;
-    double4_32a *dn = nullptr; // FP32 path: double records for the walk's re-decisions
     double2 *swing_partial = nullptr;
     SpeedState *st = nullptr;
     int *status = nullptr;
@@ -148,7 +147,6 @@ template <class R> struct Layout : LayoutBase {
             visits = mem.get<int>(nn - 1);
             agg = mem.get<Agg<R>>(nn - 1);
             nodes = mem.get<BHNode<R>>(nn - 1);
-            if (sizeof(R) == 4) dn = mem.get<double4_32a>(nn - 1);
         } else {
             packed = mem.get<R4>(nn);
         }
@@ -258,7 +256,7 @@ template <class R> struct Layout : LayoutBase {
                                                      status);
         karras_tree(s, n, key, child, range, parent, rope, visits);
         k_aggregate<R><<<ceil_div(n, 256), 256, 0, s>>>(n, psort, child, parent, range, rope,
-                                                        visits, agg, nodes, dn, status);
+                                                        visits, agg, nodes, status);
     }
     void launch_repulsion()
     {
@@ -266,24 +264,24 @@ template <class R> struct Layout : LayoutBase {
             if (walk == WALK_WARP) {
                 if (adjust)
                     k_traverse_warp<R, true><<<ceil_div(n, 256), 256, 0, s>>>(
-                        n, scaling, theta2, theta2d, psort, nodes, dn, rope, order, f, status);
+                        n, scaling, theta2, theta2d, psort, nodes, agg, rope, order, f, status);
                 else
                     k_traverse_warp<R, false><<<ceil_div(n, 256), 256, 0, s>>>(
-                        n, scaling, theta2, theta2d, psort, nodes, dn, rope, order, f, status);
+                        n, scaling, theta2, theta2d, psort, nodes, agg, rope, order, f, status);
             } else if (walk == WALK_THREAD) {
                 if (adjust)
                     k_traverse<R, true, 6><<<ceil_div(n, 256), 256, 0, s>>>(
-                        n, scaling, theta2, theta2d, psort, nodes, dn, rope, order, f, status);
+                        n, scaling, theta2, theta2d, psort, nodes, agg, rope, order, f, status);
                 else
                     k_traverse<R, false, 6><<<ceil_div(n, 256), 256, 0, s>>>(
-                        n, scaling, theta2, theta2d, psort, nodes, dn, rope, order, f, status);
+                        n, scaling, theta2, theta2d, psort, nodes, agg, rope, order, f, status);
             } else {
                 if (adjust)
                     k_traverse<R, true, 1><<<ceil_div(n, 256), 256, 0, s>>>(
-                        n, scaling, theta2, theta2d, psort, nodes, dn, rope, order, f, status);
+                        n, scaling, theta2, theta2d, psort, nodes, agg, rope, order, f, status);
                 else
                     k_traverse<R, false, 1><<<ceil_div(n, 256), 256, 0, s>>>(
-                        n, scaling, theta2, theta2d, psort, nodes, dn, rope, order, f, status);
+                        n, scaling, theta2, theta2d, psort, nodes, agg, rope, order, f, status);
             }
         } else {
             k_pack<R><<<ceil_div(n, 256), 256, 0, s>>>(n, adjust, pos, mass, size, packed);
@@ -521,7 +519,7 @@ template <class R> struct Layout : LayoutBase {
         launch_tree();
         cudaMemsetAsync(counts, 0, 2 * sizeof(unsigned long long), s);
         k_traverse_count<R><<<ceil_div(n, 256), 256, 0, s>>>(n, theta2, theta2d, psort, nodes,
-                                                             dn, rope, counts);
+                                                             agg, rope, counts);
         unsigned long long h[2] = {0, 0};
         cudaMemcpyAsync(h, counts, sizeof(h), cudaMemcpyDeviceToHost, s);
         FA2_TRY(cudaStreamSynchronize(s), "the computation on the GPU failed", 1);
