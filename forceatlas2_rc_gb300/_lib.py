@@ -66,6 +66,8 @@ def load(build_if_missing: bool = False):
         "fa2cu_layout_bytes": (C.c_double, [C.c_void_p]),
         "fa2cu_layout_close": (None, [C.c_void_p]),
         "fa2cu_build_info": (C.c_char_p, []),
+        "fa2cu_morton_order_noalloc": (C.c_int, [C.c_int, C.c_void_p, C.c_void_p,
+                                                 C.c_void_p, C.c_void_p]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -92,5 +94,5 @@ EXPORTED = (
     "fa2cu_layout_phase_times", "fa2cu_layout_tree",
     "fa2cu_layout_traversal_counts", "fa2cu_layout_option",
     "fa2cu_layout_bytes",
-    "fa2cu_layout_close", "fa2cu_build_info",
+    "fa2cu_layout_close", "fa2cu_build_info", "fa2cu_morton_order_noalloc",
 )

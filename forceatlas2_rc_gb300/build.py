@@ -34,6 +34,8 @@ UNITS = {
     # FP64 path: no contraction, IEEE division / square root (parity with the
     # reference's src/forceatlas2.c)
     "inst_f64.cu": ["-fmad=false", "-prec-div=true", "-prec-sqrt=true"],
+    # the allocation-free Morton order (FP32 positions)
+    "noalloc.cu": ["-ftz=true", "-prec-div=false", "-prec-sqrt=false"],
 }
 
 

@@ -86,6 +86,23 @@ double fa2cu_layout_bytes(const fa2cu_layout *L);
 
 void fa2cu_layout_close(fa2cu_layout *L);
 
+/* Morton codes and stable Morton order of n nodes whose positions are
+ * already on the device, without allocating any memory: the one entry point
+ * for callers that cannot call cudaMalloc (their device memory belongs to
+ * another allocator, or they cannot afford an allocation's synchronisation
+ * or failure once started). It has no counterpart in the reference.
+ *   pos    device, n interleaved (x, y) floats;
+ *   key    device, n uint32: the sorted Morton codes (16 bits per axis);
+ *   order  device, n uint32: node indices in Morton order, ties by index;
+ *   stream the cudaStream_t to run on (NULL: the default stream).
+ * 1 <= n <= 2^20, larger n is an error. Its scratch is a static device array
+ * of the library (about 8.3 MB per GPU, held until exit) shared by every
+ * call: calls that overlap on the GPU race. The first call on a device looks
+ * the array up on that device; make it before any stream capture. Returns 0,
+ * or non-zero with a message for fa2_gpu_error(). */
+int fa2cu_morton_order_noalloc(int n, const float *pos, uint32_t *key,
+                               uint32_t *order, void *stream);
+
 /* Library build description (compile flags and architecture). */
 const char *fa2cu_build_info(void);
 
