@@ -192,6 +192,39 @@ def run_reference(args):
     return 0
 
 
+def run_exact(args):
+    """The all-pairs repulsion kernel alone (fa2_gpu_repulse_exact's
+    kernel, through a resident exact layout): 100,000 nodes, FP32, pairs/s
+    and the FP32-pipe rate it implies (20 FLOP per pair, the n-body
+    convention)."""
+    import torch
+    from forceatlas2_rc_gb300 import graphs
+    from forceatlas2_rc_gb300.layout import REPULSION_EXACT, Graph, Layout
+    n = 20_000 if args.small else 100_000
+    e = np.zeros(0, np.int32)
+    g = Graph(n, e, e, np.zeros(0))
+    pos = graphs.uniform_positions(n, -1000.0, 1000.0, seed=3)
+    L = Layout(g, pos, precision="single", repulsion=REPULSION_EXACT,
+               scaling=2.0, gravity=1.0)
+    L.iterate(max(args.warmup, 1))
+    L.sync()
+    if args.profile_only:
+        L.close()
+        return 0
+    reps = max(3, args.steps // 10)
+    ph = L.phase_times(reps)
+    ms = ph["repulsion"] / reps
+    pairs = float(n) * n
+    tflops = 20.0 * pairs / (ms / 1000.0) / 1e12
+    print(json.dumps({"workload": f"exact all-pairs repulsion, n={n}, FP32",
+                      "kernel": "k_exact<float, 0, 2>", "launch_ms": ms,
+                      "pairs_per_s": pairs / (ms / 1000.0),
+                      "fp32_tflops_20flop_convention": tflops,
+                      "n": n}), flush=True)
+    L.close()
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -204,11 +237,16 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--profile-only", action="store_true",
                     help="warm-up and a few iterations only (for ncu)")
+    ap.add_argument("--workload", default="sbm1m", choices=["sbm1m", "exact"],
+                    help="sbm1m: the headline line; exact: all-pairs repulsion "
+                         "kernel alone on 100,000 nodes (FP32 pipe figures)")
     ap.add_argument("--walk", default="thread", choices=["warp", "thread", "wide"],
                     help="Barnes-Hut walk (identical forces)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "exact":
+        return run_exact(args)
 
     ws, rank, local = dist_env()
     import torch

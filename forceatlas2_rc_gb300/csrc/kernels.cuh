@@ -679,19 +679,31 @@ k_attract(int n, R gravity, int strong, int linlog, int adjust,
     }
     const R si = adjust ? size[i] : R(0);
     const int e1 = off[i + 1];
-    for (int e = off[i]; e < e1; e++) {
-        const Inc<R> c = inc[e];
-        const typename RT<R>::R2 q = pos[c.j];
-        const R xd = xi - q.x, yd = yi - q.y;
-        R g = -c.coef;
-        if (adjust || linlog) {
-            R dist = fsqrt(xd * xd + yd * yd);
-            if (adjust) dist -= si + size[c.j];
-            if (!(dist > R(0))) continue;
-            if (linlog) g *= fdiv(flog1p(dist), dist);
+    // incidences in edge order; the loads of four are issued before any of
+    // their neighbours' positions is needed (memory-level parallelism), and
+    // the sum keeps the order
+    constexpr int U = 4;
+    for (int e0 = off[i]; e0 < e1; e0 += U) {
+        Inc<R> c[U];
+        typename RT<R>::R2 q[U];
+#pragma unroll
+        for (int u = 0; u < U; u++) c[u] = inc[e0 + u < e1 ? e0 + u : e0];
+#pragma unroll
+        for (int u = 0; u < U; u++) q[u] = pos[c[u].j];
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            if (e0 + u >= e1) break;
+            const R xd = xi - q[u].x, yd = yi - q[u].y;
+            R g = -c[u].coef;
+            if (adjust || linlog) {
+                R dist = fsqrt(xd * xd + yd * yd);
+                if (adjust) dist -= si + size[c[u].j];
+                if (!(dist > R(0))) continue;
+                if (linlog) g *= fdiv(flog1p(dist), dist);
+            }
+            ax += xd * g;
+            ay += yd * g;
         }
-        ax += xd * g;
-        ay += yd * g;
     }
     f[i] = mk2<R>(ax, ay);
 }
@@ -1068,7 +1080,7 @@ k_exact(int n, R scaling, const typename RT<R>::R4 *__restrict__ nodes,
     uint64_t *bar = reinterpret_cast<uint64_t *>(smem + 2 * TILE * sizeof(R4));
     __shared__ int failed;
 
-    R xi[IPT], yi[IPT], mi[IPT], si[IPT], ax[IPT], ay[IPT];
+    R xi[IPT], yi[IPT], mi[IPT], si[IPT], smi[IPT], ax[IPT], ay[IPT];
     const int i0 = blockIdx.x * (FA2_EXACT_THREADS * IPT) + threadIdx.x;
 #pragma unroll
     for (int u = 0; u < IPT; u++) {
@@ -1078,6 +1090,7 @@ k_exact(int n, R scaling, const typename RT<R>::R4 *__restrict__ nodes,
         yi[u] = p.y;
         mi[u] = p.z;
         si[u] = p.w;
+        smi[u] = scaling * p.z;
         ax[u] = ay[u] = R(0);
     }
     const int ntiles = (n + TILE - 1) / TILE;
@@ -1112,16 +1125,34 @@ k_exact(int n, R scaling, const typename RT<R>::R4 *__restrict__ nodes,
         }
         const R4 *q = tile + b * TILE;
         const int cnt = min(TILE, n - t * TILE);
+        if constexpr (sizeof(R) == 4 && !ADJUST) {
+            // FP32: 9 FP32-pipe operations and one MUFU reciprocal per pair,
+            // with the thread's scaling * m_i hoisted out of the loop
 #pragma unroll 4
-        for (int jj = 0; jj < cnt; jj++) {
-            const R4 p = q[jj];
+            for (int jj = 0; jj < cnt; jj++) {
+                const R4 p = q[jj];
 #pragma unroll
-            for (int u = 0; u < IPT; u++) {
-                const R xd = xi[u] - p.x, yd = yi[u] - p.y;
-                const R g = rep_factor<R, ADJUST>(xd * xd + yd * yd, mi[u] * p.z,
-                                                  si[u] + p.w, scaling);
-                ax[u] += xd * g;
-                ay[u] += yd * g;
+                for (int u = 0; u < IPT; u++) {
+                    const float xd = xi[u] - p.x, yd = yi[u] - p.y;
+                    const float d2 = fmaf(xd, xd, yd * yd);
+                    const float r = __fdividef(1.0f, d2);
+                    const float g = d2 > 0.0f ? smi[u] * p.z * r : 0.0f;
+                    ax[u] = fmaf(xd, g, ax[u]);
+                    ay[u] = fmaf(yd, g, ay[u]);
+                }
+            }
+        } else {
+#pragma unroll 4
+            for (int jj = 0; jj < cnt; jj++) {
+                const R4 p = q[jj];
+#pragma unroll
+                for (int u = 0; u < IPT; u++) {
+                    const R xd = xi[u] - p.x, yd = yi[u] - p.y;
+                    const R g = rep_factor<R, ADJUST>(xd * xd + yd * yd, mi[u] * p.z,
+                                                      si[u] + p.w, scaling);
+                    ax[u] += xd * g;
+                    ay[u] += yd * g;
+                }
             }
         }
         __syncthreads(); // every thread is done with buffer b

@@ -14,7 +14,7 @@
 // Limits and sharing:
 //   - at most NOALLOC_MAX_N = 2^20 nodes; larger n is rejected with a
 //     message, nothing launched;
-//   - g_scratch (about 8.3 MB) exists on every GPU that loads the library and
+//   - g_scratch (about 9 MB) exists on every GPU that loads the library and
 //     stays there until the process exits;
 //   - every call shares it and it keeps the last call's contents: calls that
 //     overlap on the GPU (on different streams, or from several host

@@ -7,9 +7,9 @@
 
 namespace fa2cu {
 
-// Keys per block of the sort: 256 threads x 16 keys.
+// Keys per block of the sort: 256 threads x 8 keys.
 constexpr int SORT_THREADS = 256;
-constexpr int SORT_ITEMS = 16;
+constexpr int SORT_ITEMS = 8;
 constexpr int SORT_TILE = SORT_THREADS * SORT_ITEMS;
 
 // Scratch of a sort of n pairs: the ping-pong buffers and the per-block

@@ -96,7 +96,7 @@ void fa2cu_layout_close(fa2cu_layout *L);
  *   order  device, n uint32: node indices in Morton order, ties by index;
  *   stream the cudaStream_t to run on (NULL: the default stream).
  * 1 <= n <= 2^20, larger n is an error. Its scratch is a static device array
- * of the library (about 8.3 MB per GPU, held until exit) shared by every
+ * of the library (about 9 MB per GPU, held until exit) shared by every
  * call: calls that overlap on the GPU race. The first call on a device looks
  * the array up on that device; make it before any stream capture. Returns 0,
  * or non-zero with a message for fa2_gpu_error(). */
