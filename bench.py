@@ -225,6 +225,134 @@ def run_exact(args):
     return 0
 
 
+BATCH_WORKLOAD = ("4096 independent graphs, alternately Erdos-Renyi and "
+                  "islands of 40 nodes, sizes log-uniform in [50, 20000], mean "
+                  "degree uniform in [4, 16] per graph, unit weights; scaling 2, "
+                  "gravity 1, theta 1.2; exact repulsion below the autotuned "
+                  "crossover, Barnes-Hut above; FP32 with per-graph FP64 speed "
+                  "state; 500 iterations each")
+
+
+def batch_workload(count: int, seed: int = 11):
+    from forceatlas2_rc_gb300 import graphs
+    from forceatlas2_rc_gb300.layout import Graph
+    rng = np.random.default_rng(seed)
+    sizes = np.exp(rng.uniform(np.log(50.0), np.log(20000.0), count)).astype(int)
+    degs = rng.uniform(4.0, 16.0, count)
+    gs, ps = [], []
+    for i in range(count):
+        n = int(sizes[i])
+        gen = graphs.erdos_renyi if i % 2 == 0 else graphs.island_graph
+        _, a, b = gen(n, float(degs[i]), seed=100 + i)
+        gs.append(Graph(n, a, b, np.ones(len(a))))
+        r = 10.0 * np.sqrt(n)
+        ps.append(graphs.uniform_positions(n, -r, r, seed=5000 + i))
+    return gs, ps
+
+
+def run_batch(args):
+    """Config of many small graphs: layouts/s of the batched engine (one
+    persistent launch, CUDA-graph replayed) against the single-graph engine
+    called once per graph on the same GPU."""
+    import torch
+    from forceatlas2_rc_gb300.batch import Batch, tune
+    from forceatlas2_rc_gb300.layout import REPULSION_BH, REPULSION_EXACT, Layout
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    count = 256 if args.small else 4096
+    iters = 100 if args.small else 500
+    t0 = time.perf_counter()
+    gs, ps = batch_workload(count)
+    gen_s = time.perf_counter() - t0
+    nodes = sum(g.n for g in gs)
+    t0 = time.perf_counter()
+    tuned = tune(local, "single")
+    tune_s = time.perf_counter() - t0
+    kw = dict(scaling=2.0, gravity=1.0, theta=1.2)
+
+    # e2e: upload of every graph, the layout, download of every graph
+    t0 = time.perf_counter()
+    B = Batch(gs, ps, precision="single", device=local, **kw)
+    B.iterate(iters)
+    B.sync()
+    out = [B.positions(i) for i in range(count)]
+    e2e_s = time.perf_counter() - t0
+    h2d = sum(g.inc_off.nbytes + g.inc_node.nbytes + g.inc_coef.nbytes +
+              g.mass.nbytes + 16 * g.n for g in gs)
+    d2h = sum(16 * g.n for g in gs)
+    assert all(np.isfinite(o).all() for o in out)
+    if args.profile_only:
+        B.close()
+        return 0
+
+    # value: device-resident, the graphs already in HBM
+    stream = torch.cuda.ExternalStream(B.stream, device=local)
+    for _ in range(max(args.warmup, 1)):
+        B.iterate(iters)
+    B.sync()
+    steps = max(1, min(args.steps, 3))
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    with Clocks(local) as clk:
+        ev0.record(stream)
+        for _ in range(steps):
+            B.iterate(iters)
+        ev1.record(stream)
+        ev1.synchronize()
+    B.sync()
+    ms = ev0.elapsed_time(ev1)
+    B.close()
+    value = count * steps / (ms / 1000.0)
+
+    # the single-graph engine, one graph at a time (open, iterate, fetch,
+    # close), on an evenly spaced sample of the graphs
+    pick = list(range(0, count, max(1, count // 64)))
+    t0 = time.perf_counter()
+    for i in pick:
+        rep = REPULSION_EXACT if gs[i].n < tuned["exact_below"] else REPULSION_BH
+        with Layout(gs[i], ps[i], precision="single", repulsion=rep,
+                    device=local, **kw) as L:
+            L.iterate(iters)
+            L.sync()
+            L.positions()
+    loop_s = time.perf_counter() - t0
+    loop_value = len(pick) / loop_s
+    loop_nodes = sum(gs[i].n for i in pick)
+
+    line = {
+        "metric": "layouts/s (batched, 500 iterations each)",
+        "value": value, "unit": "layouts/s", "n_gpus": 1, "steps": steps,
+        "warmup": max(args.warmup, 1), "ms_per_step": ms / steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic",
+        "config": {"workload": BATCH_WORKLOAD if not args.small else
+                   f"{count} graphs (small check)", "graphs": count,
+                   "nodes": nodes, "iterations": iters,
+                   "exact_below": tuned["exact_below"],
+                   "threads": tuned["threads"],
+                   "l2": "working set > 129 MB L2 (no flush needed)"},
+        "node_iters_per_s": nodes * iters * steps / (ms / 1000.0),
+        "e2e": {"value": count / e2e_s, "unit": "layouts/s",
+                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                "step": "Batch open (upload) + 500 iterations + positions of "
+                        "every graph"},
+        "one_graph_at_a_time": {
+            "value": loop_value, "unit": "layouts/s",
+            "sample": f"{len(pick)} of the {count} graphs ({loop_nodes} nodes), "
+                      f"fa2cu_layout open/iterate/positions/close each, "
+                      f"{loop_s:.1f} s",
+            "node_iters_per_s": loop_nodes * iters / loop_s},
+        "batched_over_loop": value / loop_value,
+        "batched_e2e_over_loop": (count / e2e_s) / loop_value,
+        "gpu_launches": steps, "autotune_s": tune_s, "generate_s": gen_s,
+        "clocks": clk.summary(),
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -237,9 +365,11 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--profile-only", action="store_true",
                     help="warm-up and a few iterations only (for ncu)")
-    ap.add_argument("--workload", default="sbm1m", choices=["sbm1m", "exact"],
+    ap.add_argument("--workload", default="sbm1m",
+                    choices=["sbm1m", "exact", "batch"],
                     help="sbm1m: the headline line; exact: all-pairs repulsion "
-                         "kernel alone on 100,000 nodes (FP32 pipe figures)")
+                         "kernel alone on 100,000 nodes (FP32 pipe figures); "
+                         "batch: 4096 graphs in one persistent launch")
     ap.add_argument("--walk", default="thread", choices=["warp", "thread", "wide"],
                     help="Barnes-Hut walk (identical forces)")
     args = ap.parse_args()
@@ -247,6 +377,8 @@ def main():
         return run_reference(args)
     if args.workload == "exact":
         return run_exact(args)
+    if args.workload == "batch":
+        return run_batch(args)
 
     ws, rank, local = dist_env()
     import torch

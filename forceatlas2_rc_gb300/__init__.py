@@ -7,8 +7,9 @@ mirrors the package's R functions for the GPU paths. See layout.py.
 from .layout import (REPULSION_BH, REPULSION_EXACT, Graph, Layout, gpu_devices,
                      layout_forceatlas2_gpu, layout_forceatlas2_large,
                      prepare_graph)
+from .batch import Batch, tune
 from . import graphs
 
 __all__ = ["gpu_devices", "layout_forceatlas2_gpu", "layout_forceatlas2_large",
            "Layout", "Graph", "prepare_graph", "graphs", "REPULSION_BH",
-           "REPULSION_EXACT"]
+           "REPULSION_EXACT", "Batch", "tune"]

@@ -22,6 +22,9 @@ struct fa2cu_layout {
     fa2cu::LayoutBase *impl;
     int n;
 };
+struct fa2cu_batch {
+    fa2cu::BatchBase *impl;
+};
 
 namespace fa2cu {
 
@@ -344,6 +347,98 @@ void fa2cu_layout_close(fa2cu_layout *L)
     if (!L) return;
     delete L->impl;
     delete L;
+}
+
+// ---- batched layouts ---------------------------------------------------------
+
+static int tuned[64][2][2]; // [device][double] -> exact_below, threads (0: not yet)
+
+int fa2cu_batch_tune(int device, int use_double, int *exact_below, int *threads)
+{
+    if (check_device(device)) return 1;
+    if (device >= 64) {
+        set_message("the autotuner supports devices 0 to 63");
+        return 1;
+    }
+    int *t = tuned[device][use_double ? 1 : 0];
+    if (!t[1]) {
+        const int rc = use_double ? tune_batch_f64(device, &t[0], &t[1])
+                                  : tune_batch_f32(device, &t[0], &t[1]);
+        if (rc) {
+            t[0] = t[1] = 0;
+            return 1;
+        }
+    }
+    *exact_below = t[0];
+    *threads = t[1];
+    return 0;
+}
+
+fa2cu_batch *fa2cu_batch_open(const fa2_full_params *graphs, int count, const double *const *pos,
+                              int exact_below, int threads)
+{
+    if (!graphs || !pos || count < 1) {
+        set_message("invalid arguments: a batch needs at least one graph");
+        return nullptr;
+    }
+    const int dev = graphs[0].device, dbl = graphs[0].use_double ? 1 : 0;
+    if (check_device(dev)) return nullptr;
+    for (int g = 0; g < count; g++) {
+        const fa2_full_params &p = graphs[g];
+        if (p.n < 1 || p.n > (1 << 26)) {
+            set_message("graph %d of the batch: between 1 and 67 million nodes", g + 1);
+            return nullptr;
+        }
+        if (!pos[g] || !p.mass || (p.adjust && !p.size)) {
+            set_message("graph %d of the batch: missing positions, masses or radii", g + 1);
+            return nullptr;
+        }
+        if (check_csr(p.n, p.inc_off, p.inc_node)) return nullptr;
+        if (p.inc_off[p.n] > 0 && !p.inc_coef) {
+            set_message("graph %d of the batch: inc_coef is missing", g + 1);
+            return nullptr;
+        }
+        if (p.device != dev || (p.use_double ? 1 : 0) != dbl) {
+            set_message("the graphs of a batch share one device and one precision");
+            return nullptr;
+        }
+    }
+    if (threads != 0 && threads != 256 && threads != 512) {
+        set_message("threads must be 256 or 512 (0: tuned)");
+        return nullptr;
+    }
+    if (exact_below < 0 || threads == 0) {
+        int eb = 0, th = 0;
+        if (fa2cu_batch_tune(dev, dbl, &eb, &th)) return nullptr;
+        if (exact_below < 0) exact_below = eb;
+        if (threads == 0) threads = th;
+    }
+    BatchBase *impl = dbl ? make_batch_f64(graphs, count, pos, exact_below, threads)
+                          : make_batch_f32(graphs, count, pos, exact_below, threads);
+    if (!impl) return nullptr;
+    fa2cu_batch *B = new fa2cu_batch;
+    B->impl = impl;
+    return B;
+}
+
+int fa2cu_batch_iterate(fa2cu_batch *B, int iterations)
+{
+    if (iterations < 0) {
+        set_message("invalid number of iterations");
+        return 1;
+    }
+    return iterations ? B->impl->iterate(iterations) : 0;
+}
+int fa2cu_batch_sync(fa2cu_batch *B) { return B->impl->sync(); }
+int fa2cu_batch_positions(fa2cu_batch *B, int g, double *pos) { return B->impl->positions(g, pos); }
+int fa2cu_batch_speed(fa2cu_batch *B, int g, double state[4]) { return B->impl->speed(g, state); }
+void *fa2cu_batch_stream(fa2cu_batch *B) { return (void *) B->impl->stream(); }
+double fa2cu_batch_bytes(const fa2cu_batch *B) { return B->impl->bytes(); }
+void fa2cu_batch_close(fa2cu_batch *B)
+{
+    if (!B) return;
+    delete B->impl;
+    delete B;
 }
 
 const char *fa2cu_build_info(void)

@@ -2,6 +2,7 @@
 // float. Built with FMA contraction and approximate division / square root
 // (-ftz=true -prec-div=false -prec-sqrt=false); the steps that must be
 // bit-exact use explicit round-to-nearest intrinsics.
+#include "batch_impl.cuh"
 #include "layout_impl.cuh"
 
 namespace fa2cu {
@@ -12,5 +13,14 @@ LayoutBase *make_layout_f32(const fa2_full_params *p, const double *pos, int rep
 RepulseBase *make_repulse_f32(int device, int n, int adjust, int bh)
 {
     return make_repulse<float>(device, n, adjust, bh);
+}
+BatchBase *make_batch_f32(const fa2_full_params *ps, int count, const double *const *pos,
+                          int exact_below, int threads)
+{
+    return make_batch<float>(ps, count, pos, exact_below, threads);
+}
+int tune_batch_f32(int device, int *exact_below, int *threads)
+{
+    return tune_batch<float>(device, exact_below, threads);
 }
 } // namespace fa2cu

@@ -2,6 +2,7 @@
 // kernels.cuh instantiated for double, built with -fmad=false and IEEE
 // division and square root so that each force is computed with the
 // operations, in the order, of the reference's src/forceatlas2.c.
+#include "batch_impl.cuh"
 #include "layout_impl.cuh"
 
 namespace fa2cu {
@@ -12,5 +13,14 @@ LayoutBase *make_layout_f64(const fa2_full_params *p, const double *pos, int rep
 RepulseBase *make_repulse_f64(int device, int n, int adjust, int bh)
 {
     return make_repulse<double>(device, n, adjust, bh);
+}
+BatchBase *make_batch_f64(const fa2_full_params *ps, int count, const double *const *pos,
+                          int exact_below, int threads)
+{
+    return make_batch<double>(ps, count, pos, exact_below, threads);
+}
+int tune_batch_f64(int device, int *exact_below, int *threads)
+{
+    return tune_batch<double>(device, exact_below, threads);
 }
 } // namespace fa2cu

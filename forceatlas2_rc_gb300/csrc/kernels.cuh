@@ -373,16 +373,31 @@ __device__ __forceinline__ float4 agg_record(const Agg<float> &q)
                        2.0f * (w * w + h * h));
 }
 
-template <class R>
-__global__ void __launch_bounds__(256)
-k_aggregate(int n, const typename RT<R>::R4 *__restrict__ psort,
-            const int2 *__restrict__ child, const int *__restrict__ parent,
-            const int2 *__restrict__ range, const int *__restrict__ rope,
-            int *__restrict__ visits, Agg<R> *__restrict__ agg,
-            BHNode<R> *__restrict__ nodes, int *__restrict__ status)
+// Arrival at region r: returns the number of children that arrived before
+// (0 or 1). acq_rel: the arriving thread's writes are visible before it
+// counts, and the second arrival sees the first's. CTA scope when one block
+// builds the whole tree (the batched engine), device scope otherwise.
+template <bool CTA> __device__ __forceinline__ int arrive(int *v)
 {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= n) return;
+    int prior;
+    if (CTA)
+        asm volatile("atom.add.acq_rel.cta.s32 %0, [%1], 1;" : "=r"(prior) : "l"(v) : "memory");
+    else
+        asm volatile("atom.add.acq_rel.gpu.s32 %0, [%1], 1;" : "=r"(prior) : "l"(v) : "memory");
+    return prior;
+}
+
+// The climb of leaf k (sorted position) of an n-node tree: every region it
+// reaches second gets its sums (agg) and its traversal record (nodes).
+template <class R, bool CTA>
+__device__ __forceinline__ void climb(int k, int n, const typename RT<R>::R4 *psort,
+                                      const int2 *child,
+                                      const int *parent,
+                                      const int2 *range,
+                                      const int *rope, int *visits,
+                                      Agg<R> *agg, BHNode<R> *nodes,
+                                      int *status)
+{
     const int nl = n - 1;
     int r = parent[nl + k];
     // a Karras tree over 32-bit keys and n < 2^27 nodes is < 64 levels deep
@@ -391,14 +406,7 @@ k_aggregate(int n, const typename RT<R>::R4 *__restrict__ psort,
             atomicOr(status + ST_ERROR, ERR_BOUNDS);
             return;
         }
-        // release: this thread's region (or leaf) is written before it
-        // arrives; acquire: the sibling's is visible to the second arrival
-        int prior;
-        asm volatile("atom.add.acq_rel.gpu.s32 %0, [%1], 1;"
-                     : "=r"(prior)
-                     : "l"(visits + r)
-                     : "memory");
-        if (prior == 0) return;
+        if (arrive<CTA>(visits + r) == 0) return;
         const int2 c = child[r];
         if (c.x < 0 || c.y < 0 || c.x >= nl + n || c.y >= nl + n) {
             atomicOr(status + ST_ERROR, ERR_BOUNDS);
@@ -415,6 +423,18 @@ k_aggregate(int n, const typename RT<R>::R4 *__restrict__ psort,
         nodes[r] = nd;
         r = parent[r];
     }
+}
+
+template <class R>
+__global__ void __launch_bounds__(256)
+k_aggregate(int n, const typename RT<R>::R4 *__restrict__ psort,
+            const int2 *__restrict__ child, const int *__restrict__ parent,
+            const int2 *__restrict__ range, const int *__restrict__ rope,
+            int *__restrict__ visits, Agg<R> *__restrict__ agg,
+            BHNode<R> *__restrict__ nodes, int *__restrict__ status)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < n) climb<R, false>(k, n, psort, child, parent, range, rope, visits, agg, nodes, status);
 }
 
 // ---- 5. Barnes-Hut traversal (pipeline.cl:329-383) -------------------------
@@ -457,17 +477,14 @@ __device__ __forceinline__ bool far_dd(const Agg<double> *a, float xi, float yi,
     return false; // the FP64 walk decides in double directly
 }
 
-template <class R, bool ADJUST, int MINB>
-__global__ void __launch_bounds__(256, MINB)
-k_traverse(int n, R scaling, R theta2, double theta2d,
-           const typename RT<R>::R4 *__restrict__ psort,
-           const BHNode<R> *__restrict__ nodes, const Agg<R> *__restrict__ agg,
-           const int *__restrict__ rope, const uint32_t *__restrict__ order,
-           typename RT<R>::R2 *__restrict__ f, int *__restrict__ status)
+// The force of the tree's walk on sorted node k of an n-node tree.
+template <class R, bool ADJUST>
+__device__ __forceinline__ typename RT<R>::R2
+walk(int k, int n, R scaling, R theta2, double theta2d,
+     const typename RT<R>::R4 *psort, const BHNode<R> *nodes,
+     const Agg<R> *agg, const int *rope, int *status)
 {
     typedef typename RT<R>::R4 R4;
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= n) return;
     const R4 me = psort[k];
     const R xi = me.x, yi = me.y, mi = me.z, si = me.w;
     R ax = R(0), ay = R(0);
@@ -519,7 +536,21 @@ k_traverse(int n, R scaling, R theta2, double theta2d,
             cur = nd.t.y;
         }
     }
-    f[order[k]] = mk2<R>(ax, ay);
+    return mk2<R>(ax, ay);
+}
+
+template <class R, bool ADJUST, int MINB>
+__global__ void __launch_bounds__(256, MINB)
+k_traverse(int n, R scaling, R theta2, double theta2d,
+           const typename RT<R>::R4 *__restrict__ psort,
+           const BHNode<R> *__restrict__ nodes, const Agg<R> *__restrict__ agg,
+           const int *__restrict__ rope, const uint32_t *__restrict__ order,
+           typename RT<R>::R2 *__restrict__ f, int *__restrict__ status)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    f[order[k]] = walk<R, ADJUST>(k, n, scaling, theta2, theta2d, psort, nodes, agg, rope,
+                                  status);
 }
 
 // The same walk, warp-synchronous. The 32 threads of a warp (neighbours in
@@ -656,15 +687,18 @@ k_traverse_count(int n, R theta2, double theta2d, const typename RT<R>::R4 *__re
 
 // ---- 6. gravity and attraction (pipeline.cl:389-429) -----------------------
 
+// Gravity and attraction on node i of a graph whose arrays start at pos,
+// mass, size (node indices of inc are relative to them), added to the
+// repulsion already in f[i].
 template <class R>
-__global__ void __launch_bounds__(256)
-k_attract(int n, R gravity, int strong, int linlog, int adjust,
-          const typename RT<R>::R2 *__restrict__ pos, const R *__restrict__ mass,
-          const R *__restrict__ size, const int *__restrict__ off,
-          const Inc<R> *__restrict__ inc, typename RT<R>::R2 *__restrict__ f)
+__device__ __forceinline__ void attract_one(int i, R gravity, int strong, int linlog, int adjust,
+                                            const typename RT<R>::R2 *pos,
+                                            const R *mass,
+                                            const R *size,
+                                            const int *off,
+                                            const Inc<R> *inc,
+                                            typename RT<R>::R2 *f)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
     const typename RT<R>::R2 p = pos[i];
     const R xi = p.x, yi = p.y;
     typename RT<R>::R2 a = f[i];
@@ -706,6 +740,17 @@ k_attract(int n, R gravity, int strong, int linlog, int adjust,
         }
     }
     f[i] = mk2<R>(ax, ay);
+}
+
+template <class R>
+__global__ void __launch_bounds__(256)
+k_attract(int n, R gravity, int strong, int linlog, int adjust,
+          const typename RT<R>::R2 *__restrict__ pos, const R *__restrict__ mass,
+          const R *__restrict__ size, const int *__restrict__ off,
+          const Inc<R> *__restrict__ inc, typename RT<R>::R2 *__restrict__ f)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) attract_one<R>(i, gravity, strong, linlog, adjust, pos, mass, size, off, inc, f);
 }
 
 // ---- 7. swinging, traction, FP64 totals and the speed update --------------

@@ -47,6 +47,28 @@ struct RepulseBase {
 RepulseBase *make_repulse_f32(int device, int n, int adjust, int barnes_hut);
 RepulseBase *make_repulse_f64(int device, int n, int adjust, int barnes_hut);
 
+struct BatchBase {
+    virtual ~BatchBase() {}
+    virtual int iterate(int iterations) = 0;
+    virtual int sync() = 0;
+    virtual int positions(int g, double *pos) = 0;
+    virtual int speed(int g, double state[4]) = 0;
+    virtual cudaStream_t stream() = 0;
+    virtual double bytes() const = 0;
+    virtual int count() const = 0;
+    int device = 0;
+};
+
+// NULL on failure (message set). exact_below: graphs of fewer nodes use the
+// exact repulsion; threads: block size (256 or 512).
+BatchBase *make_batch_f32(const fa2_full_params *ps, int count, const double *const *pos,
+                          int exact_below, int threads);
+BatchBase *make_batch_f64(const fa2_full_params *ps, int count, const double *const *pos,
+                          int exact_below, int threads);
+// Crossover and block size measured on this device (0 on success).
+int tune_batch_f32(int device, int *exact_below, int *threads);
+int tune_batch_f64(int device, int *exact_below, int *threads);
+
 // Host-side checks of caller data that the kernels index with: 0 if valid,
 // otherwise 1 with the message set.
 int check_csr(int n, const int *inc_off, const int *inc_node);

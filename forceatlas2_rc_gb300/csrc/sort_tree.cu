@@ -13,6 +13,7 @@
 //           by digit in shared memory, then writes runs of equal digits to
 //           consecutive global positions.
 #include "sort_tree.cuh"
+#include "karras.cuh"
 
 namespace fa2cu {
 
@@ -204,53 +205,13 @@ void sort_pairs(cudaStream_t s, int n, uint32_t *key, uint32_t *val, const SortS
 
 // ---- Karras tree (pipeline.cl:209-270) -------------------------------------
 
-// Length of the common prefix of sorted keys i and j, -1 outside [0, n);
-// equal keys are told apart by their indices.
-__device__ __forceinline__ int cprefix(const uint32_t *__restrict__ key, int n, int i,
-                                       uint32_t ki, int j)
-{
-    if (j < 0 || j >= n) return -1;
-    const uint32_t kj = __ldg(key + j);
-    if (ki == kj) return 32 + __clz((unsigned) (i ^ j));
-    return __clz(ki ^ kj);
-}
-
 __global__ void __launch_bounds__(256)
 k_karras(int n, const uint32_t *__restrict__ key, int2 *__restrict__ child,
          int2 *__restrict__ range, int *__restrict__ parent, int *__restrict__ rope,
          int *__restrict__ visits)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n - 1) return;
-    const uint32_t ki = __ldg(key + i);
-    const int d = cprefix(key, n, i, ki, i + 1) > cprefix(key, n, i, ki, i - 1) ? 1 : -1;
-    const int pmin = cprefix(key, n, i, ki, i - d);
-    int lmax = 2;
-    while (cprefix(key, n, i, ki, i + lmax * d) > pmin) lmax *= 2;
-    int l = 0;
-    for (int t = lmax / 2; t >= 1; t /= 2)
-        if (cprefix(key, n, i, ki, i + (l + t) * d) > pmin) l += t;
-    const int j = i + l * d;
-    const int pnode = cprefix(key, n, i, ki, j);
-    int s = 0, t = l;
-    do {
-        t = (t + 1) >> 1;
-        if (cprefix(key, n, i, ki, i + (s + t) * d) > pnode) s += t;
-    } while (t > 1);
-    const int split = i + s * d + min(d, 0);
-    const int first = min(i, j), last = max(i, j);
-    const int left = first == split ? n - 1 + split : split;
-    const int right = last == split + 1 ? n - 1 + split + 1 : split + 1;
-    child[i] = make_int2(left, right);
-    range[i] = make_int2(first, last);
-    parent[left] = i;
-    parent[right] = i;
-    rope[split] = right;
-    visits[i] = 0;
-    if (i == 0) {
-        parent[0] = -1;
-        rope[n - 1] = -1;
-    }
+    if (i < n - 1) karras_one<true>(i, n, key, child, range, parent, rope, visits);
 }
 
 void karras_tree(cudaStream_t s, int n, const uint32_t *key, int2 *child, int2 *range,

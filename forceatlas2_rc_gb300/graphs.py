@@ -138,6 +138,35 @@ def erdos_renyi(n: int, mean_degree: float, seed: int = 1):
     return n, fa, ta
 
 
+def island_graph(n: int, mean_degree: float, island: int = 40, seed: int = 1):
+    """n nodes in islands of `island` nodes (the last one smaller); each
+    within-island pair is an edge with p = mean_degree / (island - 1) (at most
+    1), and every island sends 2 edges to random other islands."""
+    rng = _rng(seed)
+    k = max(1, -(-n // island))
+    fa, ta = [], []
+    start = 0
+    for c in range(k):
+        s = min(island, n - start)
+        if s >= 2:
+            iu, ju = np.triu_indices(s, k=1)
+            pick = rng.random(iu.size) < min(1.0, mean_degree / (island - 1))
+            fa.append(iu[pick] + start)
+            ta.append(ju[pick] + start)
+        start += s
+    if k > 1:
+        src = np.repeat(np.arange(k), 2)
+        dst = (src + rng.integers(1, k, src.size)) % k
+        fa.append(src * island + rng.integers(0, island, src.size) % np.minimum(
+            island, n - src * island))
+        ta.append(dst * island + rng.integers(0, island, src.size) % np.minimum(
+            island, n - dst * island))
+    if not fa:
+        return n, np.zeros(0, np.int32), np.zeros(0, np.int32)
+    a, b = dedupe(n, np.concatenate(fa), np.concatenate(ta))
+    return n, a, b
+
+
 def uniform_positions(n: int, lo: float, hi: float, seed: int = 7):
     """Start positions uniform in [lo, hi]^2, as an (n, 2) float64 array."""
     rng = _rng(seed)

@@ -86,6 +86,41 @@ double fa2cu_layout_bytes(const fa2cu_layout *L);
 
 void fa2cu_layout_close(fa2cu_layout *L);
 
+/* ---- batched layouts --------------------------------------------------- */
+
+typedef struct fa2cu_batch fa2cu_batch;
+
+/* Lay out `count` independent graphs together, every one of them by one
+ * thread block of a persistent launch (no reference counterpart: the
+ * reference lays out one graph per call). graphs[g] describes graph g
+ * (n >= 1) with its own settings as for fa2_full_run; pos[g] holds its start
+ * positions (x then y). Device and precision are those of graphs[0].
+ * Graphs with fewer than exact_below nodes use the exact repulsion, the others
+ * Barnes-Hut over their own Morton/Karras tree; threads is the block size
+ * (256 or 512). exact_below < 0 or threads == 0: the values measured by
+ * fa2cu_batch_tune on this device. A graph's result does not depend on the
+ * other graphs of the batch. NULL on error. */
+fa2cu_batch *fa2cu_batch_open(const fa2_full_params *graphs, int count,
+                              const double *const *pos, int exact_below,
+                              int threads);
+/* Enqueue `iterations` iterations of every graph (one launch). */
+int fa2cu_batch_iterate(fa2cu_batch *B, int iterations);
+int fa2cu_batch_sync(fa2cu_batch *B);
+/* Positions of graph g (x then y). */
+int fa2cu_batch_positions(fa2cu_batch *B, int g, double *pos);
+/* Speed, efficiency and last swing / traction totals of graph g. */
+int fa2cu_batch_speed(fa2cu_batch *B, int g, double state[4]);
+void *fa2cu_batch_stream(fa2cu_batch *B);
+double fa2cu_batch_bytes(const fa2cu_batch *B);
+void fa2cu_batch_close(fa2cu_batch *B);
+
+/* The autotuner: exact-vs-Barnes-Hut crossover (in nodes) and block size of
+ * the batched engine, measured on `device` in the given precision (timed
+ * batches of Erdos-Renyi graphs of 64 to 4096 nodes). Cached per device and
+ * precision for the process. */
+int fa2cu_batch_tune(int device, int use_double, int *exact_below,
+                     int *threads);
+
 /* Morton codes and stable Morton order of n nodes whose positions are
  * already on the device, without allocating any memory: the one entry point
  * for callers that cannot call cudaMalloc (their device memory belongs to
