@@ -240,7 +240,7 @@ template <class R> struct Layout : LayoutBase {
         return 0;
     }
 
-    static constexpr int EXACT_IPT = 2;
+    static constexpr int EXACT_IPT = sizeof(R) == 4 ? 2 : 1;
 
     // ---- the steps of one iteration ----
     void launch_build()
