@@ -353,6 +353,174 @@ def run_batch(args):
     return 0
 
 
+SERVE_WORKLOAD = ("layout jobs with Poisson arrivals at 200 requests/s; sizes "
+                  "log-uniform in [1000, 2000000] nodes (rounded to the nearest "
+                  "of 10 log-spaced sizes per family), 50/50 Barabasi-Albert "
+                  "(m in 2..5) and SBM (blocks of ~1000 nodes, deg_in 12, "
+                  "deg_out 2); 30% continuations from stored coordinates with "
+                  "prevent_overlap and node_size U[1,5]; 10% pin their top-1% "
+                  "degree nodes; iterations U[200,1000]; FP32 Barnes-Hut theta "
+                  "1.2, scaling 2, gravity 1")
+
+
+def serve_pool(levels: int = 10, seed: int = 21):
+    """The graphs the jobs draw from: per family, one graph at each of
+    `levels` log-spaced sizes in [1000, 2000000]."""
+    from forceatlas2_rc_gb300 import graphs
+    from forceatlas2_rc_gb300.layout import Graph
+    sizes = np.geomspace(1e3, 2e6, levels).astype(int)
+    pool = {}
+    for k, n in enumerate(sizes):
+        m = 2 + (3 * k + 1) % 4
+        _, a, b = graphs.barabasi_albert_fast(int(n), m, seed=seed + k)
+        pool[("ba", k)] = Graph(int(n), a, b, np.ones(len(a)))
+        _, a, b = graphs.sbm(int(n), max(2, int(n) // 1000), 2.1, 12.0, 2.0,
+                             seed=seed + k)
+        pool[("sbm", k)] = Graph(int(n), a, b, np.ones(len(a)))
+    return sizes, pool
+
+
+def serve_trace(count: int, rate: float, sizes, seed: int = 5):
+    rng = np.random.default_rng(seed)
+    t = np.cumsum(rng.exponential(1.0 / rate, count))
+    ls = np.log(sizes)
+    jobs = []
+    for i in range(count):
+        kind = "ba" if rng.random() < 0.5 else "sbm"
+        k = int(np.argmin(np.abs(ls - rng.uniform(np.log(1e3), np.log(2e6)))))
+        jobs.append(dict(t=float(t[i]), kind=kind, k=k,
+                         cont=bool(rng.random() < 0.3),
+                         pin=bool(rng.random() < 0.1),
+                         iters=int(rng.integers(200, 1001)), seed=1000 + i))
+    return jobs
+
+
+def serve_inputs(jobs, pool, local):
+    """Every job's start positions and settings, made before the clock
+    starts; a continuation starts from stored coordinates (the graph after
+    30 iterations from random positions)."""
+    from forceatlas2_rc_gb300 import graphs
+    from forceatlas2_rc_gb300.layout import Layout
+    stored = {}
+    out = []
+    for j in jobs:
+        g = pool[(j["kind"], j["k"])]
+        rng = np.random.default_rng(j["seed"])
+        r = 10.0 * np.sqrt(g.n)
+        kw = dict(scaling=2.0, gravity=1.0, theta=1.2)
+        if j["cont"]:
+            key = (j["kind"], j["k"])
+            if key not in stored:
+                with Layout(g, graphs.uniform_positions(g.n, -r, r, seed=3),
+                            device=local, **kw) as L:
+                    L.iterate(30)
+                    L.sync()
+                    stored[key] = L.positions()
+            pos = stored[key]
+            kw.update(adjust=True, size=rng.uniform(1.0, 5.0, g.n))
+        else:
+            pos = graphs.uniform_positions(g.n, -r, r, seed=j["seed"])
+        if j["pin"]:
+            deg = g.mass - 1.0
+            top = np.argsort(-deg, kind="stable")[:max(1, g.n // 100)]
+            fixed = np.zeros(g.n, np.int32)
+            fixed[top] = 1
+            kw["fixed"] = fixed
+        out.append(dict(g=g, pos=pos, kw=kw))
+    return out
+
+
+def serve_pass(jobs, inputs, scale, device, max_jobs):
+    """Submit the jobs at their arrival times (x scale) to a fresh server,
+    collect every result on another thread; latency = end - arrival."""
+    import threading
+    from forceatlas2_rc_gb300 import _lib
+    from forceatlas2_rc_gb300.serve import Server
+    lib = _lib.load()
+    done = []
+    submitted = threading.Semaphore(0)
+    with Server(device=device, max_jobs=max_jobs, chunk=16) as S:
+        def collect():
+            for _ in range(len(jobs)):
+                submitted.acquire()  # a job to wait for
+                r = S.wait()
+                done.append((r[0], r[2]))
+        th = threading.Thread(target=collect)
+        th.start()
+        ids = {}
+        t0 = time.perf_counter()
+        c0 = lib.fa2_now()
+        for j, inp in zip(jobs, inputs):
+            dt = j["t"] * scale - (time.perf_counter() - t0)
+            if dt > 0:
+                time.sleep(dt)
+            jid = S.submit(inp["g"], inp["pos"], j["iters"], **inp["kw"])
+            ids[jid] = j
+            submitted.release()
+        th.join()
+        st = S.stats()
+    lat = np.array([m["t_end"] - (c0 + ids[jid]["t"] * scale) for jid, m in done])
+    queued = np.array([m["t_resident"] - m["t_submit"] for _, m in done])
+    end = max(m["t_end"] for _, m in done) - c0
+    node_iters = sum(m["n"] * m["iterations"] for _, m in done)
+    return {"jobs": len(done), "makespan_s": end,
+            "layouts_per_s": len(done) / end,
+            "node_iters_per_s": node_iters / end,
+            "p50_latency_s": float(np.percentile(lat, 50)),
+            "p99_latency_s": float(np.percentile(lat, 99)),
+            "mean_latency_s": float(lat.mean()),
+            "p50_wait_resident_s": float(np.percentile(queued, 50)),
+            "peak_footprint_gb": st["peak_footprint"] / 1e9,
+            "pool_reserved_gb": st["pool_reserved"] / 1e9,
+            "arrival_rate_per_s": 200.0 / scale, "max_jobs": max_jobs}
+
+
+def run_serve(args):
+    """Serving: continuous batching of layout jobs by the layout server,
+    against the same trace run one job at a time, plus a pass at half the
+    measured capacity."""
+    import torch
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    count = 24 if args.small else 96
+    t0 = time.perf_counter()
+    sizes, pool = serve_pool(6 if args.small else 10)
+    if args.small:
+        sizes = sizes[:4]
+    jobs = serve_trace(count, 200.0, sizes)
+    inputs = serve_inputs(jobs, pool, local)
+    prep_s = time.perf_counter() - t0
+    with Clocks(local) as clk:
+        busy = serve_pass(jobs, inputs, 1.0, local, 16)
+    one = serve_pass(jobs, inputs, 1.0, local, 1)
+    low_rate = 0.5 * busy["layouts_per_s"]
+    low_jobs = jobs[:max(8, count // 3)]
+    low = serve_pass(low_jobs, inputs[:len(low_jobs)], 200.0 / low_rate, local, 16)
+    line = {
+        "metric": "served layouts/s, p50/p99 latency", "value": busy["layouts_per_s"],
+        "unit": "layouts/s", "n_gpus": 1, "steps": busy["jobs"], "warmup": 0,
+        "ms_per_step": 1000.0 * busy["makespan_s"] / busy["jobs"],
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic",
+        "config": {"workload": SERVE_WORKLOAD, "jobs": count,
+                   "pool_sizes": [int(x) for x in sizes],
+                   "l2": "working sets > 129 MB L2 for the large jobs"},
+        "p50_latency_s": busy["p50_latency_s"], "p99_latency_s": busy["p99_latency_s"],
+        "served_200_per_s": busy, "one_job_at_a_time": one,
+        "half_capacity": low,
+        "e2e": {"value": busy["layouts_per_s"], "unit": "layouts/s",
+                "h2d_bytes_per_step": int(np.mean([
+                    i["g"].inc_off.nbytes + i["g"].inc_node.nbytes +
+                    i["g"].inc_coef.nbytes + 32 * i["g"].n for i in inputs])),
+                "d2h_bytes_per_step": int(np.mean([16 * i["g"].n for i in inputs])),
+                "step": "one job: submit (host arrays) to collected positions"},
+        "prep_s": prep_s, "clocks": clk.summary(),
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -366,10 +534,11 @@ def main():
     ap.add_argument("--profile-only", action="store_true",
                     help="warm-up and a few iterations only (for ncu)")
     ap.add_argument("--workload", default="sbm1m",
-                    choices=["sbm1m", "exact", "batch"],
+                    choices=["sbm1m", "exact", "batch", "serve"],
                     help="sbm1m: the headline line; exact: all-pairs repulsion "
                          "kernel alone on 100,000 nodes (FP32 pipe figures); "
-                         "batch: 4096 graphs in one persistent launch")
+                         "batch: 4096 graphs in one persistent launch; "
+                         "serve: the layout server on a Poisson job trace")
     ap.add_argument("--walk", default="thread", choices=["warp", "thread", "wide"],
                     help="Barnes-Hut walk (identical forces)")
     args = ap.parse_args()
@@ -379,6 +548,8 @@ def main():
         return run_exact(args)
     if args.workload == "batch":
         return run_batch(args)
+    if args.workload == "serve":
+        return run_serve(args)
 
     ws, rank, local = dist_env()
     import torch

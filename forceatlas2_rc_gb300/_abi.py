@@ -66,6 +66,12 @@ FULL_TIME_NAMES = ("total", "codes", "sort", "tree", "repulsion",
                    "attraction", "move")
 
 
+class ServerConfig(C.Structure):
+    """fa2cu_server_config (include/fa2_cuda.h)."""
+    _fields_ = [("device", C.c_int), ("hbm_budget", C.c_double),
+                ("max_jobs", C.c_int), ("chunk", C.c_int)]
+
+
 def dptr(a):
     """double* of a contiguous float64 numpy array (or NULL for None)."""
     if a is None:

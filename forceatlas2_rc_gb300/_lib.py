@@ -10,7 +10,7 @@ from __future__ import annotations
 import ctypes as C
 import os
 
-from ._abi import DevInfo, FullParams, Tree
+from ._abi import DevInfo, FullParams, ServerConfig, Tree
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libfa2cuda.so")
@@ -78,6 +78,16 @@ def load(build_if_missing: bool = False):
         "fa2cu_batch_bytes": (C.c_double, [C.c_void_p]),
         "fa2cu_batch_close": (None, [C.c_void_p]),
         "fa2cu_batch_tune": (C.c_int, [C.c_int, C.c_int, P_I, P_I]),
+        "fa2cu_server_open": (C.c_void_p, [C.POINTER(ServerConfig)]),
+        "fa2cu_server_submit": (C.c_longlong, [C.c_void_p, C.POINTER(FullParams),
+                                               P_D, C.c_int]),
+        "fa2cu_server_wait": (C.c_longlong, [C.c_void_p, C.c_longlong, C.c_double,
+                                             P_D]),
+        "fa2cu_server_collect": (C.c_int, [C.c_void_p, C.c_longlong, P_D]),
+        "fa2cu_server_stats": (C.c_int, [C.c_void_p, P_D]),
+        "fa2cu_server_close": (None, [C.c_void_p]),
+        "fa2cu_layout_footprint": (C.c_double, [C.c_int, C.c_int, C.c_int, C.c_int,
+                                                C.c_int, C.c_int]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -108,4 +118,7 @@ EXPORTED = (
     "fa2cu_batch_open", "fa2cu_batch_iterate", "fa2cu_batch_sync",
     "fa2cu_batch_positions", "fa2cu_batch_speed", "fa2cu_batch_stream",
     "fa2cu_batch_bytes", "fa2cu_batch_close", "fa2cu_batch_tune",
+    "fa2cu_server_open", "fa2cu_server_submit", "fa2cu_server_wait",
+    "fa2cu_server_collect",
+    "fa2cu_server_stats", "fa2cu_server_close", "fa2cu_layout_footprint",
 )

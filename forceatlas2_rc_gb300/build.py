@@ -36,6 +36,8 @@ UNITS = {
     "inst_f64.cu": ["-fmad=false", "-prec-div=true", "-prec-sqrt=true"],
     # the allocation-free Morton order (FP32 positions)
     "noalloc.cu": ["-ftz=true", "-prec-div=false", "-prec-sqrt=false"],
+    # the layout server (host threads over the layouts of both precisions)
+    "server.cu": [],
 }
 
 
@@ -78,7 +80,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
         objs = list(ex.map(lambda kv: _compile(kv[0], kv[1], verbose),
                            UNITS.items()))
     tmp = LIB + ".tmp"
-    cmd = [nvcc()] + ARCH + ["-shared", "-o", tmp] + objs
+    cmd = [nvcc()] + ARCH + ["-shared", "-o", tmp] + objs + ["-lpthread"]
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:
         raise RuntimeError(f"linking libfa2cuda.so failed:\n{res.stderr}")

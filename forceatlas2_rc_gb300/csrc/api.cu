@@ -28,7 +28,8 @@ struct fa2cu_batch {
 
 namespace fa2cu {
 
-static char errbuf[2048] = "";
+// one message per host thread (the serving loop runs on threads of its own)
+static thread_local char errbuf[2048] = "";
 
 void set_message(const char *fmt, ...)
 {

@@ -6,9 +6,14 @@
 #include "layout_impl.cuh"
 
 namespace fa2cu {
-LayoutBase *make_layout_f32(const fa2_full_params *p, const double *pos, int rep)
+LayoutBase *make_layout_f32(const fa2_full_params *p, const double *pos, int rep,
+                            const LayoutOpts *opts)
 {
-    return make_layout<float>(p, pos, rep);
+    return make_layout<float>(p, pos, rep, opts);
+}
+double layout_footprint_f32(int n, int ninc, int adjust, int any_fixed, int rep)
+{
+    return layout_footprint<float>(n, ninc, adjust, any_fixed, rep);
 }
 RepulseBase *make_repulse_f32(int device, int n, int adjust, int bh)
 {

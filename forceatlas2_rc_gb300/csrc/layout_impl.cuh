@@ -40,12 +40,21 @@ struct DevMem {
     double bytes = 0.0;
     bool failed = false;
     cudaError_t err = cudaSuccess;
+    // With a pool: stream-ordered allocations on `s` from `pool` (no device
+    // synchronisation on allocation or release). Dry: count bytes only.
+    cudaMemPool_t pool = nullptr;
+    cudaStream_t s = nullptr;
+    bool dry = false;
     template <class T> T *get(size_t count)
     {
         if (failed) return nullptr;
         void *p = nullptr;
         const size_t b = (count > 0 ? count : 1) * sizeof(T);
-        err = cudaMalloc(&p, b);
+        if (dry) {
+            bytes += (double) b;
+            return nullptr;
+        }
+        err = pool ? cudaMallocFromPoolAsync(&p, b, pool, s) : cudaMalloc(&p, b);
         if (err != cudaSuccess) {
             failed = true;
             return nullptr;
@@ -56,7 +65,12 @@ struct DevMem {
     }
     void release()
     {
-        for (void *p : ptrs) cudaFree(p);
+        for (void *p : ptrs) {
+            if (pool)
+                cudaFreeAsync(p, s);
+            else
+                cudaFree(p);
+        }
         ptrs.clear();
     }
 };
@@ -157,7 +171,8 @@ template <class R> struct Layout : LayoutBase {
         return 0;
     }
 
-    int open(const fa2_full_params *p, const double *xy0, int rep)
+    int open(const fa2_full_params *p, const double *xy0, int rep,
+             const LayoutOpts *opts = nullptr)
     {
         n = p->n;
         ninc = p->inc_off[n];
@@ -172,14 +187,22 @@ template <class R> struct Layout : LayoutBase {
         gravity = (R) p->gravity;
         theta2d = p->theta * p->theta;
         theta2 = (R) theta2d;
-        FA2_TRY(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking),
-                "could not create a CUDA stream", 1);
+        if (opts && opts->has_priority)
+            FA2_TRY(cudaStreamCreateWithPriority(&s, cudaStreamNonBlocking, opts->priority),
+                    "could not create a CUDA stream", 1);
+        else
+            FA2_TRY(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking),
+                    "could not create a CUDA stream", 1);
         for (auto &e : ev) FA2_TRY(cudaEventCreate(&e), "could not create a CUDA event", 1);
+        mem.pool = opts ? opts->pool : nullptr;
+        mem.s = s;
         if (alloc(rep == FA2CU_REPULSION_BH)) return 1;
 
         // the graph, once (reference src/gpu_full.c:241-287)
         {
             DevMem tmp;
+            tmp.pool = mem.pool;
+            tmp.s = s;
             double *dd = tmp.get<double>(std::max<size_t>((size_t) n, (size_t) ninc));
             int *di = tmp.get<int>((size_t) ninc);
             if (tmp.failed) {
@@ -529,17 +552,34 @@ template <class R> struct Layout : LayoutBase {
     }
 };
 
-template <class R> LayoutBase *make_layout(const fa2_full_params *p, const double *pos, int rep)
+template <class R>
+LayoutBase *make_layout(const fa2_full_params *p, const double *pos, int rep,
+                        const LayoutOpts *opts)
 {
     int dev = p->device;
     FA2_TRY(cudaSetDevice(dev), "could not use the CUDA device", nullptr);
     Layout<R> *L = new Layout<R>();
     L->device = dev;
-    if (L->open(p, pos, rep)) {
+    if (L->open(p, pos, rep, opts)) {
         delete L;
         return nullptr;
     }
     return L;
+}
+
+// Device bytes a layout holds (its buffers, counted by the allocation plan
+// itself) plus the transient staging of the graph upload at open.
+template <class R> double layout_footprint(int n, int ninc, int adjust, int any_fixed, int rep)
+{
+    Layout<R> L;
+    L.n = n;
+    L.ninc = ninc;
+    L.adjust = adjust ? 1 : 0;
+    L.any_fixed = any_fixed ? 1 : 0;
+    L.mem.dry = true;
+    L.alloc(rep == FA2CU_REPULSION_BH);
+    const double staging = (double) std::max(n, ninc) * sizeof(double) + (double) ninc * sizeof(int);
+    return L.mem.bytes + staging;
 }
 
 // ---- the repulsion backend of fa2_gpu_open (reference src/gpu.c:357-704) --

@@ -30,9 +30,23 @@ struct LayoutBase {
     int device = 0;
 };
 
+// How a layout gets its stream and memory: by default its own stream and
+// cudaMalloc; a server passes a memory pool (stream-ordered allocation) and a
+// stream priority.
+struct LayoutOpts {
+    cudaMemPool_t pool = nullptr;
+    bool has_priority = false;
+    int priority = 0;
+};
+
 // NULL on failure (message set). `pos` is x then y.
-LayoutBase *make_layout_f32(const fa2_full_params *p, const double *pos, int repulsion);
-LayoutBase *make_layout_f64(const fa2_full_params *p, const double *pos, int repulsion);
+LayoutBase *make_layout_f32(const fa2_full_params *p, const double *pos, int repulsion,
+                            const LayoutOpts *opts = nullptr);
+LayoutBase *make_layout_f64(const fa2_full_params *p, const double *pos, int repulsion,
+                            const LayoutOpts *opts = nullptr);
+// Device bytes of a layout of n nodes and ninc incidences, staging included.
+double layout_footprint_f32(int n, int ninc, int adjust, int any_fixed, int repulsion);
+double layout_footprint_f64(int n, int ninc, int adjust, int any_fixed, int repulsion);
 
 struct RepulseBase {
     virtual ~RepulseBase() {}

@@ -93,6 +93,36 @@ def barabasi_albert(n: int, m: int = 3, seed: int = 1):
     return n, src, dst
 
 
+def barabasi_albert_fast(n: int, m: int = 3, seed: int = 1):
+    """Preferential attachment for large n, vectorised: nodes join in
+    batches of about 1/16 of the nodes present, each drawing m endpoints
+    uniformly from the endpoint list as it stood when its batch began (the
+    degree-proportional choice of barabasi_albert, up to that lag); repeated
+    picks are dropped. Node m starts as the hub of a star on 0..m-1."""
+    rng = _rng(seed)
+    if n <= m:
+        raise ValueError("barabasi_albert_fast needs n > m")
+    ends = np.empty(2 * m * (n - m), dtype=np.int64)
+    ends[:m] = m
+    ends[m:2 * m] = np.arange(m)
+    ne = 2 * m
+    src = [np.full(m, m, np.int64)]
+    dst = [np.arange(m, dtype=np.int64)]
+    v = m + 1
+    while v < n:
+        b = min(n - v, max(1, v // 16))
+        new = np.repeat(np.arange(v, v + b, dtype=np.int64), m)
+        tgt = ends[rng.integers(0, ne, b * m)]
+        src.append(new)
+        dst.append(tgt)
+        ends[ne:ne + b * m] = new
+        ends[ne + b * m:ne + 2 * b * m] = tgt
+        ne += 2 * b * m
+        v += b
+    a, t = dedupe(n, np.concatenate(src), np.concatenate(dst))
+    return n, a, t
+
+
 def pa_test_graph(n: int, seed: int = 42):
     """The package tests' graph shape: preferential attachment with m = 2."""
     if n < 3:

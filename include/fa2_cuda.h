@@ -121,6 +121,64 @@ void fa2cu_batch_close(fa2cu_batch *B);
 int fa2cu_batch_tune(int device, int use_double, int *exact_below,
                      int *threads);
 
+/* ---- serving ------------------------------------------------------------ */
+
+/* A layout server (no reference counterpart: the reference runs one layout
+ * per call, start to end). Jobs are submitted from any host thread; an
+ * admission thread makes each one resident on the device (graph, positions,
+ * tree buffers and speed state, in a memory pool of the server) while the
+ * estimated device footprint of the resident jobs stays within the budget
+ * and fewer than max_jobs are resident; a scheduling thread interleaves the
+ * jobs' iterations, `chunk` at a time, each job on a stream of its own
+ * whose priority rises as its work (nodes x iterations) falls. A job's
+ * result is the same as the single-layout path's for its inputs, whatever
+ * else runs beside it. */
+typedef struct fa2cu_server fa2cu_server;
+
+typedef struct {
+    int device;
+    double hbm_budget; /* bytes the resident jobs may hold; <= 0: 80 % of the
+                          device's free memory at open */
+    int max_jobs;      /* jobs resident at once; <= 0: 16 */
+    int chunk;         /* iterations enqueued per job at a time; <= 0: 16 */
+} fa2cu_server_config;
+
+fa2cu_server *fa2cu_server_open(const fa2cu_server_config *cfg);
+
+/* Submit a layout job: the graph and settings as for fa2_full_run (its
+ * p->iterations iterations in p->use_double precision; p->device, profile,
+ * source and interrupted are ignored), start positions pos (x then y),
+ * repulsion FA2CU_REPULSION_BH or FA2CU_REPULSION_EXACT. Everything is
+ * copied before the call returns. Returns the job's id (>= 0), or -1 with a
+ * message (invalid job, or a footprint above the whole budget). */
+long long fa2cu_server_submit(fa2cu_server *S, const fa2_full_params *p,
+                              const double *pos, int repulsion);
+
+/* Wait up to timeout_s seconds (< 0: no limit) for job `id` to end, or for
+ * any ended job not yet claimed if id < 0, and claim it. info[8]: submit,
+ * resident and end times (fa2_now's clock), status (0 done, 1 failed), n,
+ * iterations, footprint bytes, final speed. Returns the id, -1 on timeout,
+ * -2 if there is no such job (or, for id < 0, none left to claim). */
+long long fa2cu_server_wait(fa2cu_server *S, long long id, double timeout_s,
+                            double info[8]);
+
+/* Copy an ended job's final positions into pos (2n doubles, x then y; may be
+ * NULL) and release the job. 0, or 1 with a message: the job has not ended
+ * (or was collected), or it failed (its own message). */
+int fa2cu_server_collect(fa2cu_server *S, long long id, double *pos);
+
+/* out[8]: jobs queued, resident, done, failed; footprint bytes resident now
+ * and at most so far; the budget; device bytes reserved by the pool. */
+int fa2cu_server_stats(fa2cu_server *S, double out[8]);
+
+/* Stop the threads, drop the jobs not collected, release the pool. */
+void fa2cu_server_close(fa2cu_server *S);
+
+/* Device bytes a layout of n nodes and ninc incidences holds (its buffers
+ * and the staging of the graph upload): the server's admission estimate. */
+double fa2cu_layout_footprint(int n, int ninc, int adjust, int any_fixed,
+                              int use_double, int repulsion);
+
 /* Morton codes and stable Morton order of n nodes whose positions are
  * already on the device, without allocating any memory: the one entry point
  * for callers that cannot call cudaMalloc (their device memory belongs to
