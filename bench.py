@@ -688,6 +688,42 @@ def main():
                "step": "fa2_full_run, 1000 iterations, host buffers (pinned)",
                "s_per_layout": dt / calls}
 
+        # the same layout from the edge list: fa2cu_full_run_edges prepares
+        # masses and incidence lists on the device (the host's O(m)
+        # preparation of C_forceatlas2_large moves into the timed call)
+        from forceatlas2_rc_gb300.layout import _EdgeOnly
+        ea, t1 = pinned(np.ascontiguousarray(a, dtype=np.int32))
+        eb, t2 = pinned(np.ascontiguousarray(b, dtype=np.int32))
+        ew, t3 = pinned(np.ones(len(a)))
+        keep += [t1, t2, t3]
+        pe, keep3 = _params(_EdgeOnly(n), host["size"], host["fixed"], 2.0, 1.0, 1.2,
+                            1.0, False, True, False, iters, local, False)
+        from forceatlas2_rc_gb300._abi import iptr
+        run_e = lambda: lib.fa2cu_full_run_edges(  # noqa: E731
+            C.byref(pe), len(a), iptr(ea), iptr(eb), dptr(ew), 1, dptr(host["pos"]),
+            dptr(times))
+        host["pos"][:] = xy0
+        assert run_e() == 0, _lib.error()
+        if pg:
+            pg.barrier()
+        t0 = time.perf_counter()
+        for _ in range(calls):
+            host["pos"][:] = xy0
+            assert run_e() == 0, _lib.error()
+        dte = time.perf_counter() - t0
+        if pg:
+            t = torch.tensor([dte], device=f"cuda:{local}")
+            pg.all_reduce(t, op=pg.ReduceOp.MAX)
+            dte = float(t.item())
+        e2e["from_edges"] = {
+            "value": ws * n * iters * calls / dte, "unit": UNIT,
+            "h2d_bytes_per_step": int(ea.nbytes + eb.nbytes + ew.nbytes +
+                                      host["pos"].nbytes),
+            "d2h_bytes_per_step": int(d2h),
+            "step": "fa2cu_full_run_edges (edge list in, graph prepared on "
+                    "the device), 1000 iterations, host buffers (pinned)",
+            "s_per_layout": dte / calls}
+
     # ---- roofline of the dominant kernel (the traversal) -------------------
     peaks, kind = measured_peaks()
     t_trav = ph["repulsion"] / 1000.0
@@ -712,10 +748,17 @@ def main():
         threads = os.cpu_count() or 1
         iters = 40 if not args.small else 10
         cv, cdt = cpu_sample(n, a, b, iters, threads)
+        import oracle
+        t0 = time.perf_counter()
+        oracle.prepare_large(n, a, b, np.ones(len(a)), outbound=True)
+        prep_s = time.perf_counter() - t0
         cpu = {"value": cv, "unit": UNIT, "cores": threads, "kind": "port",
                "sample": f"{iters} iterations of the full {n}-node workload "
                          f"(after 1 warm-up), C_forceatlas2 quadtree engine, "
-                         f"{cdt:.1f} s"}
+                         f"{cdt:.1f} s",
+               "graph_prep_s": prep_s,
+               "graph_prep": "C_forceatlas2_large's host preparation (masses, "
+                             "incidence lists), oracle restatement, 1 core"}
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws,

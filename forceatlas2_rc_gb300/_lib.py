@@ -88,6 +88,12 @@ def load(build_if_missing: bool = False):
         "fa2cu_server_close": (None, [C.c_void_p]),
         "fa2cu_layout_footprint": (C.c_double, [C.c_int, C.c_int, C.c_int, C.c_int,
                                                 C.c_int, C.c_int]),
+        "fa2cu_graph_prep": (C.c_longlong, [C.c_int, C.c_int, C.c_int, P_I, P_I, P_D,
+                                            C.c_int, P_D, P_I, P_I, P_D]),
+        "fa2cu_layout_open_edges": (C.c_void_p, [C.POINTER(FullParams), C.c_int, P_I,
+                                                 P_I, P_D, C.c_int, P_D, C.c_int]),
+        "fa2cu_full_run_edges": (C.c_int, [C.POINTER(FullParams), C.c_int, P_I, P_I,
+                                           P_D, C.c_int, P_D, P_D]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -121,4 +127,5 @@ EXPORTED = (
     "fa2cu_server_open", "fa2cu_server_submit", "fa2cu_server_wait",
     "fa2cu_server_collect",
     "fa2cu_server_stats", "fa2cu_server_close", "fa2cu_layout_footprint",
+    "fa2cu_graph_prep", "fa2cu_layout_open_edges", "fa2cu_full_run_edges",
 )

@@ -38,6 +38,9 @@ UNITS = {
     "noalloc.cu": ["-ftz=true", "-prec-div=false", "-prec-sqrt=false"],
     # the layout server (host threads over the layouts of both precisions)
     "server.cu": [],
+    # graph preparation on the device (integer work and IEEE double
+    # coefficients, as the reference's host code)
+    "prep.cu": ["-fmad=false", "-prec-div=true", "-prec-sqrt=true"],
 }
 
 

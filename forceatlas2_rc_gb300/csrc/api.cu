@@ -11,6 +11,7 @@
 #include <vector>
 
 #include "session.h"
+#include "prep.cuh"
 #include "common.cuh"
 
 // Opaque handles of the C interface.
@@ -450,6 +451,59 @@ const char *fa2cu_build_info(void)
 
 // ---- fa2_full_run (reference src/gpu_full.c:164-532) ------------------------
 
+// The iterations of fa2_full_run on an open layout, then its positions.
+// Interruptions are polled about every 10^6 units of work, as the reference
+// (src/gpu_full.c:403-411): one chunk of iterations runs while the next is
+// queued, and the host checks p->interrupted() each time a chunk ends.
+static int run_full(fa2cu_layout *L, const fa2_full_params *p, int ninc, double *pos,
+                    double *times)
+{
+    const double start = fa2_now();
+    const int n = p->n;
+    const double per_it = (double) n + (double) ninc;
+    int chunk = (int) (1e6 / per_it);
+    if (chunk < 1) chunk = 1;
+    int status = 0;
+    double ms[FA2_FULL_NTIMES] = {0, 0, 0, 0, 0, 0, 0};
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+    for (auto &e : ev)
+        if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) {
+            set_message("could not create a CUDA event");
+            status = 1;
+        }
+    cudaStream_t s = L->impl->stream();
+    long long c = 0;
+    for (int it = 0; it < p->iterations && !status; c++) {
+        const int k = p->iterations - it < chunk ? p->iterations - it : chunk;
+        if (c >= 2 && cudaEventSynchronize(ev[c & 1]) != cudaSuccess) {
+            set_message("the computation on the GPU failed");
+            status = 1;
+            break;
+        }
+        if (c >= 2 && p->interrupted && p->interrupted()) {
+            L->impl->sync();
+            set_message("the layout was interrupted");
+            status = 1;
+            break;
+        }
+        if (p->profile)
+            status = L->impl->phase_times(k, ms);
+        else
+            status = L->impl->iterate(k);
+        if (!status) cudaEventRecord(ev[c & 1], s);
+        it += k;
+    }
+    if (!status) status = L->impl->sync();
+    if (!status) status = L->impl->positions(pos);
+    if (!status) {
+        times[FA2_FULL_T_TOTAL] = fa2_now() - start;
+        for (int k = 1; k < FA2_FULL_NTIMES; k++) times[k] = ms[k] / 1000.0;
+    }
+    for (auto &e : ev)
+        if (e) cudaEventDestroy(e);
+    return status;
+}
+
 int fa2_full_run(const fa2_full_params *p, double *pos, double *times)
 {
     for (int i = 0; i < FA2_FULL_NTIMES; i++) times[i] = 0.0;
@@ -459,37 +513,143 @@ int fa2_full_run(const fa2_full_params *p, double *pos, double *times)
     }
     fa2cu_layout *L = fa2cu_layout_open(p, pos, FA2CU_REPULSION_BH);
     if (!L) return 1;
-    const double start = fa2_now();
-    const int n = p->n;
-    const double per_it = (double) n + (double) p->inc_off[n];
-    // interruptions are polled every ~1e6 units of work, as the reference
-    // (src/gpu_full.c:403-411); the device never waits for the host between
-    // iterations.
-    int chunk = (int) (1e6 / per_it);
-    if (chunk < 1) chunk = 1;
-    int status = 0;
-    double ms[FA2_FULL_NTIMES] = {0, 0, 0, 0, 0, 0, 0};
-    for (int it = 0; it < p->iterations && !status;) {
-        const int k = p->iterations - it < chunk ? p->iterations - it : chunk;
-        if (p->profile)
-            status = L->impl->phase_times(k, ms);
-        else
-            status = L->impl->iterate(k);
-        it += k;
-        if (!status && p->interrupted && it < p->iterations && p->interrupted()) {
-            L->impl->sync();
-            set_message("the layout was interrupted");
-            status = 1;
-        }
-    }
-    if (!status) status = L->impl->sync();
-    if (!status) status = L->impl->positions(pos);
-    if (!status) {
-        times[FA2_FULL_T_TOTAL] = fa2_now() - start;
-        for (int k = 1; k < FA2_FULL_NTIMES; k++) times[k] = ms[k] / 1000.0;
-    }
+    const int status = run_full(L, p, p->inc_off[p->n], pos, times);
     fa2cu_layout_close(L);
     return status;
+}
+
+// ---- graphs given as edge lists (preparation on the device) -------------------
+
+// Largest edge count of the device preparation (its 2m sort entries and a
+// sort tile stay within int indexing).
+static const int PREP_MAX_EDGES = (1 << 30) - (1 << 20);
+
+static int check_edges(int n, int m, const int *from, const int *to, const double *w)
+{
+    if (m < 0 || m > PREP_MAX_EDGES) {
+        set_message("the edge list must have between 0 and %d edges", PREP_MAX_EDGES);
+        return 1;
+    }
+    if (m > 0 && (!from || !to || !w)) {
+        set_message("invalid arguments: the edge list is missing");
+        return 1;
+    }
+    (void) n;
+    return 0;
+}
+
+fa2cu_layout *fa2cu_layout_open_edges(const fa2_full_params *p, int m, const int *from,
+                                      const int *to, const double *w, int outbound,
+                                      const double *pos, int repulsion)
+{
+    if (!p || !pos) {
+        set_message("invalid arguments");
+        return nullptr;
+    }
+    if (repulsion != FA2CU_REPULSION_BH && repulsion != FA2CU_REPULSION_EXACT) {
+        set_message("unknown repulsion %d", repulsion);
+        return nullptr;
+    }
+    const int nmin = repulsion == FA2CU_REPULSION_EXACT ? 1 : 2;
+    if (p->n < nmin || p->n > (1 << 26)) {
+        set_message("the all-GPU layout handles between 2 and 67 million nodes");
+        return nullptr;
+    }
+    if (p->adjust && !p->size) {
+        set_message("invalid arguments: radii are required with adjust");
+        return nullptr;
+    }
+    if (check_edges(p->n, m, from, to, w)) return nullptr;
+    if (check_device(p->device)) return nullptr;
+    EdgeList E;
+    E.m = m;
+    E.from = from;
+    E.to = to;
+    E.w = w;
+    E.outbound = outbound ? 1 : 0;
+    LayoutBase *impl = p->use_double ? make_layout_f64(p, pos, repulsion, nullptr, &E)
+                                     : make_layout_f32(p, pos, repulsion, nullptr, &E);
+    if (!impl) return nullptr;
+    fa2cu_layout *L = new fa2cu_layout;
+    L->impl = impl;
+    L->n = p->n;
+    return L;
+}
+
+int fa2cu_full_run_edges(const fa2_full_params *p, int m, const int *from, const int *to,
+                         const double *w, int outbound, double *pos, double *times)
+{
+    for (int i = 0; i < FA2_FULL_NTIMES; i++) times[i] = 0.0;
+    if (p->iterations < 0) {
+        set_message("invalid number of iterations");
+        return 1;
+    }
+    fa2cu_layout *L =
+        fa2cu_layout_open_edges(p, m, from, to, w, outbound, pos, FA2CU_REPULSION_BH);
+    if (!L) return 1;
+    // incidences: at most 2m (self-loops have none); only the interrupt
+    // polling interval depends on it
+    const int status = run_full(L, p, 2 * m, pos, times);
+    fa2cu_layout_close(L);
+    return status;
+}
+
+long long fa2cu_graph_prep(int device, int n, int m, const int *from, const int *to,
+                           const double *w, int outbound, double *mass, int *inc_off,
+                           int *inc_node, double *inc_coef)
+{
+    if (n < 1 || n > (1 << 26)) {
+        set_message("the graph must have between 1 and 67 million nodes");
+        return -1;
+    }
+    if (check_edges(n, m, from, to, w)) return -1;
+    if (check_device(device)) return -1;
+    FA2_TRY(cudaSetDevice(device), "could not use the CUDA device", -1);
+    cudaStream_t s = nullptr;
+    FA2_TRY(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking), "could not create a CUDA stream",
+            -1);
+    DevMem mem;
+    const size_t m1 = (size_t) (m > 0 ? m : 1);
+    int *df = mem.get<int>(m1), *dt = mem.get<int>(m1);
+    double *dw = mem.get<double>(m1), *dm = mem.get<double>((size_t) n);
+    int *doff = mem.get<int>((size_t) n + 1), *dnode = mem.get<int>(2 * m1);
+    double *dcoef = mem.get<double>(2 * m1);
+    PrepScratch ws;
+    prep_scratch(mem, n, m, ws);
+    long long got = -1;
+    if (mem.failed) {
+        set_cuda_error("could not allocate memory on the device", mem.err);
+    } else {
+        int rc = 0;
+        if (m > 0) {
+            rc |= cudaMemcpyAsync(df, from, (size_t) m * sizeof(int), cudaMemcpyHostToDevice, s);
+            rc |= cudaMemcpyAsync(dt, to, (size_t) m * sizeof(int), cudaMemcpyHostToDevice, s);
+            rc |= cudaMemcpyAsync(dw, w, (size_t) m * sizeof(double), cudaMemcpyHostToDevice, s);
+        }
+        if (rc) set_message("could not send the graph to the device");
+        else got = prep_graph(s, n, m, df, dt, dw, outbound, dm, doff, dnode, dcoef, ws);
+        if (got >= 0) {
+            rc = 0;
+            rc |= cudaMemcpyAsync(mass, dm, (size_t) n * sizeof(double), cudaMemcpyDeviceToHost, s);
+            rc |= cudaMemcpyAsync(inc_off, doff, ((size_t) n + 1) * sizeof(int),
+                                  cudaMemcpyDeviceToHost, s);
+            if (got > 0) {
+                rc |= cudaMemcpyAsync(inc_node, dnode, (size_t) got * sizeof(int),
+                                      cudaMemcpyDeviceToHost, s);
+                rc |= cudaMemcpyAsync(inc_coef, dcoef, (size_t) got * sizeof(double),
+                                      cudaMemcpyDeviceToHost, s);
+            }
+            rc |= cudaStreamSynchronize(s);
+            if (rc) {
+                set_message("could not fetch the prepared graph");
+                got = -1;
+            }
+        }
+    }
+    cudaStreamSynchronize(s);
+    mem.release();
+    cudaStreamDestroy(s);
+    return got;
 }
 
 } // extern "C"

@@ -7,9 +7,9 @@
 
 namespace fa2cu {
 LayoutBase *make_layout_f64(const fa2_full_params *p, const double *pos, int rep,
-                            const LayoutOpts *opts)
+                            const LayoutOpts *opts, const EdgeList *edges)
 {
-    return make_layout<double>(p, pos, rep, opts);
+    return make_layout<double>(p, pos, rep, opts, edges);
 }
 double layout_footprint_f64(int n, int ninc, int adjust, int any_fixed, int rep)
 {

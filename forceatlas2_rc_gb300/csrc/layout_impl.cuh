@@ -21,7 +21,9 @@
 #include <time.h>
 #include <vector>
 
+#include "devmem.cuh"
 #include "kernels.cuh"
+#include "prep.cuh"
 #include "session.h"
 #include "sort_tree.cuh"
 
@@ -35,46 +37,6 @@ inline double now_s()
 }
 
 // Device allocations of a session, released together.
-struct DevMem {
-    std::vector<void *> ptrs;
-    double bytes = 0.0;
-    bool failed = false;
-    cudaError_t err = cudaSuccess;
-    // With a pool: stream-ordered allocations on `s` from `pool` (no device
-    // synchronisation on allocation or release). Dry: count bytes only.
-    cudaMemPool_t pool = nullptr;
-    cudaStream_t s = nullptr;
-    bool dry = false;
-    template <class T> T *get(size_t count)
-    {
-        if (failed) return nullptr;
-        void *p = nullptr;
-        const size_t b = (count > 0 ? count : 1) * sizeof(T);
-        if (dry) {
-            bytes += (double) b;
-            return nullptr;
-        }
-        err = pool ? cudaMallocFromPoolAsync(&p, b, pool, s) : cudaMalloc(&p, b);
-        if (err != cudaSuccess) {
-            failed = true;
-            return nullptr;
-        }
-        ptrs.push_back(p);
-        bytes += (double) b;
-        return (T *) p;
-    }
-    void release()
-    {
-        for (void *p : ptrs) {
-            if (pool)
-                cudaFreeAsync(p, s);
-            else
-                cudaFree(p);
-        }
-        ptrs.clear();
-    }
-};
-
 template <class R> struct Layout : LayoutBase {
     typedef typename RT<R>::R2 R2;
     typedef typename RT<R>::R4 R4;
@@ -171,11 +133,74 @@ template <class R> struct Layout : LayoutBase {
         return 0;
     }
 
+    // The graph from its edge list, prepared on the device (prep.cu): the
+    // masses, the incidence lists and their coefficients in double, then
+    // converted to the layout's precision.
+    int prepare_edges(const fa2_full_params *p, const EdgeList &E)
+    {
+        DevMem tmp;
+        tmp.pool = mem.pool;
+        tmp.s = s;
+        const size_t m1 = (size_t) std::max(E.m, 1);
+        int *from = tmp.get<int>(m1), *to = tmp.get<int>(m1);
+        double *w = tmp.get<double>(m1);
+        double *dmass = tmp.get<double>((size_t) n);
+        int *dnode = tmp.get<int>(2 * m1);
+        double *dcoef = tmp.get<double>(std::max(2 * m1, (size_t) n));
+        PrepScratch ws;
+        prep_scratch(tmp, n, E.m, ws);
+        if (tmp.failed) {
+            tmp.release();
+            set_cuda_error("could not allocate memory on the device", tmp.err);
+            return 1;
+        }
+        int rc = 0;
+        auto up = [&](void *dst, const void *src, size_t b) {
+            if (!rc && b) rc = cudaMemcpyAsync(dst, src, b, cudaMemcpyHostToDevice, s) != cudaSuccess;
+        };
+        up(from, E.from, (size_t) E.m * sizeof(int));
+        up(to, E.to, (size_t) E.m * sizeof(int));
+        up(w, E.w, (size_t) E.m * sizeof(double));
+        if (rc) {
+            tmp.release();
+            set_cuda_error("could not send the graph to the device", cudaGetLastError());
+            return 1;
+        }
+        const long long got =
+            prep_graph(s, n, E.m, from, to, w, E.outbound, dmass, inc_off, dnode, dcoef, ws);
+        if (got < 0) {
+            cudaStreamSynchronize(s);
+            tmp.release();
+            return 1;
+        }
+        ninc = (int) got;
+        k_real_in<R><<<ceil_div(n, 256), 256, 0, s>>>(n, dmass, mass);
+        if (ninc > 0) k_inc_in<R><<<ceil_div(ninc, 256), 256, 0, s>>>(ninc, dnode, dcoef, inc);
+        if (adjust) {
+            up(dcoef, p->size, (size_t) n * sizeof(double));
+            if (!rc) k_real_in<R><<<ceil_div(n, 256), 256, 0, s>>>(n, dcoef, size);
+        }
+        if (any_fixed) {
+            std::vector<uint8_t> f8((size_t) n);
+            for (int i = 0; i < n; i++) f8[i] = p->fixed[i] != 0;
+            up(fixed, f8.data(), (size_t) n);
+        }
+        if (!rc) rc = cudaStreamSynchronize(s) != cudaSuccess;
+        tmp.release();
+        if (rc) {
+            set_cuda_error("could not send the graph to the device", cudaGetLastError());
+            return 1;
+        }
+        return 0;
+    }
+
     int open(const fa2_full_params *p, const double *xy0, int rep,
-             const LayoutOpts *opts = nullptr)
+             const LayoutOpts *opts = nullptr, const EdgeList *edges = nullptr)
     {
         n = p->n;
-        ninc = p->inc_off[n];
+        // from an edge list: at most two incidences per edge until the
+        // preparation on the device has counted them
+        ninc = edges ? 2 * edges->m : p->inc_off[n];
         repulsion = rep;
         adjust = p->adjust ? 1 : 0;
         strong = p->strong ? 1 : 0;
@@ -198,8 +223,11 @@ template <class R> struct Layout : LayoutBase {
         mem.s = s;
         if (alloc(rep == FA2CU_REPULSION_BH)) return 1;
 
-        // the graph, once (reference src/gpu_full.c:241-287)
-        {
+        // the graph, once (reference src/gpu_full.c:241-287), or prepared on
+        // the device from its edge list
+        if (edges) {
+            if (prepare_edges(p, *edges)) return 1;
+        } else {
             DevMem tmp;
             tmp.pool = mem.pool;
             tmp.s = s;
@@ -554,13 +582,13 @@ template <class R> struct Layout : LayoutBase {
 
 template <class R>
 LayoutBase *make_layout(const fa2_full_params *p, const double *pos, int rep,
-                        const LayoutOpts *opts)
+                        const LayoutOpts *opts, const EdgeList *edges)
 {
     int dev = p->device;
     FA2_TRY(cudaSetDevice(dev), "could not use the CUDA device", nullptr);
     Layout<R> *L = new Layout<R>();
     L->device = dev;
-    if (L->open(p, pos, rep, opts)) {
+    if (L->open(p, pos, rep, opts, edges)) {
         delete L;
         return nullptr;
     }

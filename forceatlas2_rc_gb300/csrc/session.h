@@ -39,11 +39,21 @@ struct LayoutOpts {
     int priority = 0;
 };
 
+// A graph given as its edge list (0-based ends, weights): the layout then
+// prepares masses and incidence lists on the device, and p's inc_off,
+// inc_node, inc_coef and mass are not read.
+struct EdgeList {
+    int m = 0;
+    const int *from = nullptr, *to = nullptr;
+    const double *w = nullptr;
+    int outbound = 0;
+};
+
 // NULL on failure (message set). `pos` is x then y.
 LayoutBase *make_layout_f32(const fa2_full_params *p, const double *pos, int repulsion,
-                            const LayoutOpts *opts = nullptr);
+                            const LayoutOpts *opts = nullptr, const EdgeList *edges = nullptr);
 LayoutBase *make_layout_f64(const fa2_full_params *p, const double *pos, int repulsion,
-                            const LayoutOpts *opts = nullptr);
+                            const LayoutOpts *opts = nullptr, const EdgeList *edges = nullptr);
 // Device bytes of a layout of n nodes and ninc incidences, staging included.
 double layout_footprint_f32(int n, int ninc, int adjust, int any_fixed, int repulsion);
 double layout_footprint_f64(int n, int ninc, int adjust, int any_fixed, int repulsion);

@@ -183,11 +183,12 @@ k_sort_scatter(int n, int shift, const uint32_t *__restrict__ kin, const uint32_
 
 size_t sort_scratch_counts(int n) { return 256 * (size_t) ceil_div(n, SORT_TILE); }
 
-void sort_pairs(cudaStream_t s, int n, uint32_t *key, uint32_t *val, const SortScratch &w)
+void sort_pairs_passes(cudaStream_t s, int n, uint32_t *key, uint32_t *val,
+                       const SortScratch &w, int passes, uint32_t **kout, uint32_t **vout)
 {
     const int nb = ceil_div(n, SORT_TILE);
     uint32_t *ka = key, *va = val, *kb = w.key_b, *vb = w.val_b;
-    for (int pass = 0; pass < 4; pass++) {
+    for (int pass = 0; pass < passes; pass++) {
         const int shift = 8 * pass;
         k_sort_hist<<<nb, SORT_THREADS, 0, s>>>(n, shift, ka, w.counts, nb);
         k_sort_scan<<<256, 1024, 0, s>>>(nb, w.counts, w.digit_total);
@@ -200,7 +201,14 @@ void sort_pairs(cudaStream_t s, int n, uint32_t *key, uint32_t *val, const SortS
         va = vb;
         vb = t;
     }
-    // four passes: the result is back in key / val
+    *kout = ka;
+    *vout = va;
+}
+
+void sort_pairs(cudaStream_t s, int n, uint32_t *key, uint32_t *val, const SortScratch &w)
+{
+    uint32_t *k = nullptr, *v = nullptr;
+    sort_pairs_passes(s, n, key, val, w, 4, &k, &v); // four passes: back in key / val
 }
 
 // ---- Karras tree (pipeline.cl:209-270) -------------------------------------

@@ -26,6 +26,12 @@ size_t sort_scratch_counts(int n); // entries of `counts`
 void sort_pairs(cudaStream_t s, int n, uint32_t *key, uint32_t *val,
                 const SortScratch &w);
 
+// The same with `passes` (1..4) passes of 8 bits, for keys below
+// 2^(8 passes); the sorted pairs are left in (*kout, *vout), either key / val
+// or the scratch buffers.
+void sort_pairs_passes(cudaStream_t s, int n, uint32_t *key, uint32_t *val,
+                       const SortScratch &w, int passes, uint32_t **kout, uint32_t **vout);
+
 // Karras tree over n >= 2 sorted keys: child[r] = (left, right),
 // range[r] = (first, last) for the n-1 regions, parent of the 2n-1 tree nodes
 // (leaves are n-1+k), rope[p] = right child of the region split after sorted

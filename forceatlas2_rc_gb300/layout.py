@@ -151,6 +151,43 @@ def prepare_graph(n, edges, weights=None, dissuade_hubs=False, **wkw) -> Graph:
     return Graph(n, frm, to, w, outbound=dissuade_hubs)
 
 
+class _EdgeOnly:
+    """A graph known by its edge list only (the device prepares the rest):
+    placeholder arrays for the unused CSR fields of the parameters."""
+
+    def __init__(self, n):
+        self.n = n
+        self.inc_off = np.zeros(n + 1, np.int32)
+        self.inc_node = np.zeros(1, np.int32)
+        self.inc_coef = np.zeros(1)
+        self.mass = np.ones(n)
+
+
+def prepare_graph_device(n, frm, to, w, dissuade_hubs=False, device=0) -> Graph:
+    """Graph with masses and incidence lists prepared on the device
+    (fa2cu_graph_prep); the same arrays as Graph() builds on the host."""
+    frm = np.ascontiguousarray(frm, dtype=np.int32)
+    to = np.ascontiguousarray(to, dtype=np.int32)
+    w = np.ascontiguousarray(w, dtype=np.float64)
+    m = len(frm)
+    mass = np.zeros(n)
+    off = np.zeros(n + 1, np.int32)
+    node = np.zeros(max(2 * m, 1), np.int32)
+    coef = np.zeros(max(2 * m, 1))
+    got = _lib.load().fa2cu_graph_prep(int(device), int(n), m, iptr(frm), iptr(to),
+                                       dptr(w), int(dissuade_hubs), dptr(mass),
+                                       iptr(off), iptr(node), dptr(coef))
+    if got < 0:
+        raise RuntimeError(_lib.error())
+    g = Graph.__new__(Graph)
+    g.n = n
+    g.mass = mass
+    g.inc_off = off
+    g.inc_node = node[:got].copy() if got > 0 else np.zeros(1, np.int32)
+    g.inc_coef = coef[:got].copy() if got > 0 else np.zeros(1)
+    return g
+
+
 def _params(g: Graph, size, fixed, scaling, gravity, theta, jitter, strong,
             linlog, adjust, iterations, device, use_double, profile=False):
     n = g.n
@@ -308,7 +345,8 @@ def _resolve_device(device) -> int:
 
 def _common(n, edges, iterations, scaling_ratio, gravity, jitter_tolerance,
             theta, node_size, init, fixed, seed, weights, edge_weight_influence,
-            normalize_weights, invert_weights, dissuade_hubs, flags):
+            normalize_weights, invert_weights, dissuade_hubs, flags,
+            host_graph=True):
     iterations = int(_number(iterations, "iterations", 0, whole=True))
     gravity = _number(gravity, "gravity", 0)
     _number(edge_weight_influence, "edge_weight_influence", 0)
@@ -344,10 +382,13 @@ def _common(n, edges, iterations, scaling_ratio, gravity, jitter_tolerance,
     else:
         pos = np.asarray(init, dtype=np.float64)
         _cols(pos, n)
-    g = prepare_graph(n, edges, weights, dissuade_hubs,
-                      edge_weight_influence=edge_weight_influence,
-                      normalize_weights=normalize_weights,
-                      invert_weights=invert_weights)
+    frm, to = _edges(n, edges)
+    w = edge_weights(len(frm), weights, edge_weight_influence=edge_weight_influence,
+                     normalize_weights=normalize_weights,
+                     invert_weights=invert_weights)
+    # the host preparation, or the edge list for the device's
+    g = Graph(n, frm, to, w, outbound=dissuade_hubs) if host_graph else \
+        (frm, to, np.ascontiguousarray(w, dtype=np.float64))
     return iterations, gravity, jitter_tolerance, theta, scaling_ratio, size, \
         fx, pos, g
 
@@ -360,9 +401,16 @@ def layout_forceatlas2_large(n, edges, iterations=1000, scaling_ratio=None,
                              normalize_weights=False, invert_weights=False,
                              init=None, fixed=None, jitter_tolerance=1.0,
                              theta=1.2, device=None, precision="single",
-                             seed: Optional[int] = None, timings=False):
-    """The all-GPU layout through ``fa2_full_run``; returns an (n, 2) array
-    (and the phase timings in seconds when ``timings``)."""
+                             seed: Optional[int] = None, timings=False,
+                             prep="device"):
+    """The all-GPU layout; returns an (n, 2) array (and the phase timings in
+    seconds when ``timings``). ``prep="host"`` prepares masses and incidence
+    lists on the host and calls ``fa2_full_run``, as the package's
+    ``C_forceatlas2_large``; ``prep="device"`` (the default) passes the edge
+    list to ``fa2cu_full_run_edges``, which prepares them on the device --
+    the same numbers bit for bit."""
+    if prep not in ("device", "host"):
+        raise ValueError("`prep` must be \"device\" or \"host\"")
     if precision not in ("single", "double"):
         raise ValueError("'arg' should be one of \"single\", \"double\"")
     flags = dict(strong_gravity=strong_gravity, linlog=linlog,
@@ -373,7 +421,8 @@ def layout_forceatlas2_large(n, edges, iterations=1000, scaling_ratio=None,
      g) = _common(n, edges, iterations, scaling_ratio, gravity,
                   jitter_tolerance, theta, node_size, init, fixed, seed,
                   weights, edge_weight_influence, normalize_weights,
-                  invert_weights, dissuade_hubs, flags)
+                  invert_weights, dissuade_hubs, flags,
+                  host_graph=prep == "host" or n < 2)
     if n == 0:
         return np.zeros((0, 2))
     dev = _resolve_device(device)
@@ -388,12 +437,22 @@ def layout_forceatlas2_large(n, edges, iterations=1000, scaling_ratio=None,
             L.iterate(iterations)
             L.sync()
             return L.positions()
-    p, keep = _params(g, size, fx, scaling, gravity, theta, jitter,
-                      strong_gravity, linlog, prevent_overlap, iterations, dev,
-                      precision == "double", profile=timings)
     xy = _cols(pos, n)
     t = np.zeros(FA2_FULL_NTIMES)
-    rc = _lib.load().fa2_full_run(C.byref(p), dptr(xy), dptr(t))
+    if prep == "host":
+        p, keep = _params(g, size, fx, scaling, gravity, theta, jitter,
+                          strong_gravity, linlog, prevent_overlap, iterations,
+                          dev, precision == "double", profile=timings)
+        rc = _lib.load().fa2_full_run(C.byref(p), dptr(xy), dptr(t))
+    else:
+        frm, to, w = g
+        p, keep = _params(_EdgeOnly(n), size, fx, scaling, gravity, theta,
+                          jitter, strong_gravity, linlog, prevent_overlap,
+                          iterations, dev, precision == "double",
+                          profile=timings)
+        rc = _lib.load().fa2cu_full_run_edges(
+            C.byref(p), len(frm), iptr(frm), iptr(to), dptr(w),
+            int(dissuade_hubs), dptr(xy), dptr(t))
     if rc != 0:
         raise RuntimeError(_lib.error())
     out = xy.reshape(2, n).T.copy()

@@ -86,6 +86,38 @@ double fa2cu_layout_bytes(const fa2cu_layout *L);
 
 void fa2cu_layout_close(fa2cu_layout *L);
 
+/* ---- graphs given as edge lists ---------------------------------------- */
+
+/* The preparation C_forceatlas2_large does on the host before fa2_full_run
+ * (reference src/forceatlas2.c:868-902), on the device: mass = 1 + degree
+ * (a self-loop counts twice), the symmetric incidence lists with each node's
+ * incidences in edge order (self-loops have none), coefficient
+ * coef * w[e] (/ mass[from[e]] when outbound, coef = the mean mass; else
+ * coef = 1). from / to: m edges, 0-based; w: m weights (after the R layer's
+ * weight transformations). Outputs on the host: mass[n], inc_off[n + 1],
+ * inc_node and inc_coef (at most 2m). Returns the number of incidences, or -1
+ * with a message ("edge %d refers to a node that does not exist", the first
+ * such edge numbered from 1, as the reference). No reference counterpart as
+ * a separate call. */
+long long fa2cu_graph_prep(int device, int n, int m, const int *from,
+                           const int *to, const double *w, int outbound,
+                           double *mass, int *inc_off, int *inc_node,
+                           double *inc_coef);
+
+/* fa2cu_layout_open with the graph given as its edge list, prepared on the
+ * device as fa2cu_graph_prep (p's inc_off, inc_node, inc_coef and mass are
+ * not read). */
+fa2cu_layout *fa2cu_layout_open_edges(const fa2_full_params *p, int m,
+                                      const int *from, const int *to,
+                                      const double *w, int outbound,
+                                      const double *pos, int repulsion);
+
+/* fa2_full_run with the graph given as its edge list (C_forceatlas2_large's
+ * host preparation moved to the device); the same results bit for bit. */
+int fa2cu_full_run_edges(const fa2_full_params *p, int m, const int *from,
+                         const int *to, const double *w, int outbound,
+                         double *pos, double *times);
+
 /* ---- batched layouts --------------------------------------------------- */
 
 typedef struct fa2cu_batch fa2cu_batch;
