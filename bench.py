@@ -47,6 +47,8 @@ WORKLOAD = ("SBM n=1,000,000, 1000 power-law blocks (exp 2.1), deg_in 12, "
 # kernels of one Barnes-Hut iteration: bbox, morton, 4 x (hist, scan,
 # scatter), gather, karras, aggregate, traverse, attract, swing, apply
 LAUNCHES_PER_ITER = 21
+# Barnes-Hut walks (fa2cu_layout_option "walk"): identical forces
+WALKS = {"warp": 0, "thread": 1, "wide": 2, "pair": 3, "quad": 4}
 # algorithmic HBM bytes per node of the traversal: psort record 16, order 4,
 # force write 8 (FP32)
 TRAVERSE_HBM_BYTES_PER_NODE = 28
@@ -539,7 +541,8 @@ def main():
                          "kernel alone on 100,000 nodes (FP32 pipe figures); "
                          "batch: 4096 graphs in one persistent launch; "
                          "serve: the layout server on a Poisson job trace")
-    ap.add_argument("--walk", default="thread", choices=["warp", "thread", "wide"],
+    ap.add_argument("--walk", default="thread",
+                    choices=["warp", "thread", "wide", "pair", "quad"],
                     help="Barnes-Hut walk (identical forces)")
     args = ap.parse_args()
     if args.impl == "reference":
@@ -571,7 +574,7 @@ def main():
     kw = dict(scaling=2.0, gravity=1.0, theta=1.2, linlog=True, device=local)
     L = Layout(g, pos, precision="single", repulsion=REPULSION_BH, **kw)
     if args.walk != "thread":
-        L.option("walk", {"warp": 0, "wide": 2}[args.walk])
+        L.option("walk", WALKS[args.walk])
     stream = torch.cuda.ExternalStream(L.stream, device=local)
 
     if args.profile_only:
@@ -735,7 +738,9 @@ def main():
                 "traffic": None,
                 "kernel": {"warp": "k_traverse_warp<float>",
                            "thread": "k_traverse<float, 6>",
-                           "wide": "k_traverse<float, 1>"}[args.walk],
+                           "wide": "k_traverse<float, 1>",
+                           "pair": "k_traverse_multi<float, 2>",
+                           "quad": "k_traverse_multi<float, 4>"}[args.walk],
                 "peak_kind": f"{kind} (HBM copy)",
                 "launch_ms": ph["repulsion"],
                 "l2_request_bytes": l2_bytes,

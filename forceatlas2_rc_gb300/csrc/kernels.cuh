@@ -553,6 +553,122 @@ k_traverse(int n, R scaling, R theta2, double theta2d,
                                   status);
 }
 
+// The walk of P sorted nodes k0 .. k0+cnt-1 (cnt <= P, neighbours in
+// Morton order) by one thread. The thread walks the union of the nodes'
+// walks, in the same preorder, loading each region once for all of them.
+// Each node keeps its own decisions: after it approximates a region, it
+// stays inactive until the walk reaches that region's skip link (the first
+// region after its subtree), where its own walk would go next; the nodes
+// near a small region sum its node pairs together, each skipping itself.
+// Every node therefore computes the interactions of its own walk, in the
+// same order, with the same arithmetic: the forces are those of walk().
+template <class R, bool ADJUST, int P>
+__device__ __forceinline__ void
+walk_multi(int k0, int cnt, int n, R scaling, R theta2, double theta2d,
+           const typename RT<R>::R4 *psort, const BHNode<R> *nodes, const Agg<R> *agg,
+           const int *rope, const uint32_t *order, typename RT<R>::R2 *f, int *status)
+{
+    typedef typename RT<R>::R4 R4;
+    constexpr int ACTIVE = -2;
+    R xi[P], yi[P], mi[P], si[P], ax[P], ay[P];
+    int resume[P]; // ACTIVE, or the walk position at which the node resumes
+#pragma unroll
+    for (int u = 0; u < P; u++) {
+        const R4 me = psort[u < cnt ? k0 + u : k0];
+        xi[u] = me.x;
+        yi[u] = me.y;
+        mi[u] = me.z;
+        si[u] = me.w;
+        ax[u] = ay[u] = R(0);
+        resume[u] = u < cnt ? ACTIVE : -1; // a missing node never resumes
+    }
+    const int nl = n - 1;
+    int cur = 0, j = 0, jend = -1;
+    unsigned pairs = 0; // nodes summing the current range
+    const int cap = 4 * n + 64;
+    for (int step = 0;; step++) {
+        if (step > cap || cur >= nl + n || jend >= n) {
+            atomicOr(status + ST_ERROR, ERR_BOUNDS);
+            break;
+        }
+        if (j <= jend) {
+            const R4 q = psort[j];
+#pragma unroll
+            for (int u = 0; u < P; u++) {
+                if (((pairs >> u) & 1u) && j != k0 + u) {
+                    const R xd = xi[u] - q.x, yd = yi[u] - q.y;
+                    const R g = rep_factor<R, ADJUST>(xd * xd + yd * yd, mi[u] * q.z,
+                                                      si[u] + q.w, scaling);
+                    ax[u] += xd * g;
+                    ay[u] += yd * g;
+                }
+            }
+            ++j;
+            continue;
+        }
+        if (cur < 0) break;
+        unsigned act = 0;
+#pragma unroll
+        for (int u = 0; u < P; u++) {
+            if (resume[u] == cur) resume[u] = ACTIVE;
+            if (resume[u] == ACTIVE) act |= 1u << u;
+        }
+        if (cur >= nl) { // a single node
+            j = jend = cur - nl;
+            pairs = act;
+            cur = rope[j];
+            continue;
+        }
+        const BHNode<R> nd = nodes[cur];
+        unsigned nearm = 0;
+#pragma unroll
+        for (int u = 0; u < P; u++) {
+            if (!((act >> u) & 1u)) continue;
+            const R xd = xi[u] - nd.c.x, yd = yi[u] - nd.c.y;
+            const R d2 = xd * xd + yd * yd;
+            const R lhs = d2 * theta2;
+            bool far = lhs > nd.c.w;
+            if (sizeof(R) == 4 && fabs_r(lhs - nd.c.w) <= R(DECIDE_BAND) * nd.c.w)
+                far = far_dd(agg + cur, (float) xi[u], (float) yi[u], theta2d);
+            if (far) {
+                const R g = fdiv(scaling * (mi[u] * nd.c.z), d2);
+                ax[u] += xd * g;
+                ay[u] += yd * g;
+                resume[u] = nd.t.y;
+            } else {
+                nearm |= 1u << u;
+            }
+        }
+        if (nearm == 0) {
+            cur = nd.t.y;
+        } else if (nd.t.w - nd.t.z >= 8) {
+            cur = nd.t.x;
+        } else {
+            j = nd.t.z;
+            jend = nd.t.w;
+            pairs = nearm;
+            cur = nd.t.y;
+        }
+    }
+#pragma unroll
+    for (int u = 0; u < P; u++)
+        if (u < cnt) f[order[k0 + u]] = mk2<R>(ax[u], ay[u]);
+}
+
+template <class R, bool ADJUST, int P>
+__global__ void __launch_bounds__(256)
+k_traverse_multi(int n, R scaling, R theta2, double theta2d,
+                 const typename RT<R>::R4 *__restrict__ psort,
+                 const BHNode<R> *__restrict__ nodes, const Agg<R> *__restrict__ agg,
+                 const int *__restrict__ rope, const uint32_t *__restrict__ order,
+                 typename RT<R>::R2 *__restrict__ f, int *__restrict__ status)
+{
+    const int k0 = (blockIdx.x * blockDim.x + threadIdx.x) * P;
+    if (k0 >= n) return;
+    walk_multi<R, ADJUST, P>(k0, min(P, n - k0), n, scaling, theta2, theta2d, psort, nodes,
+                             agg, rope, order, f, status);
+}
+
 // The same walk, warp-synchronous. The 32 threads of a warp (neighbours in
 // Morton order) walk the tree together, one region per step, so that every
 // load is a broadcast and no branch diverges; a region is opened when any

@@ -326,6 +326,22 @@ template <class R> struct Layout : LayoutBase {
                 else
                     k_traverse<R, false, 6><<<ceil_div(n, 256), 256, 0, s>>>(
                         n, scaling, theta2, theta2d, psort, nodes, agg, rope, order, f, status);
+            } else if (walk == WALK_PAIR) {
+                const int grid = ceil_div(ceil_div(n, 2), 256);
+                if (adjust)
+                    k_traverse_multi<R, true, 2><<<grid, 256, 0, s>>>(
+                        n, scaling, theta2, theta2d, psort, nodes, agg, rope, order, f, status);
+                else
+                    k_traverse_multi<R, false, 2><<<grid, 256, 0, s>>>(
+                        n, scaling, theta2, theta2d, psort, nodes, agg, rope, order, f, status);
+            } else if (walk == WALK_QUAD) {
+                const int grid = ceil_div(ceil_div(n, 4), 256);
+                if (adjust)
+                    k_traverse_multi<R, true, 4><<<grid, 256, 0, s>>>(
+                        n, scaling, theta2, theta2d, psort, nodes, agg, rope, order, f, status);
+                else
+                    k_traverse_multi<R, false, 4><<<grid, 256, 0, s>>>(
+                        n, scaling, theta2, theta2d, psort, nodes, agg, rope, order, f, status);
             } else {
                 if (adjust)
                     k_traverse<R, true, 1><<<ceil_div(n, 256), 256, 0, s>>>(
@@ -543,7 +559,8 @@ template <class R> struct Layout : LayoutBase {
     int option(const char *name, double value) override
     {
         if (!strcmp(name, "walk") &&
-            (value == WALK_WARP || value == WALK_THREAD || value == WALK_THREAD_WIDE)) {
+            (value == WALK_WARP || value == WALK_THREAD || value == WALK_THREAD_WIDE ||
+             value == WALK_PAIR || value == WALK_QUAD)) {
             walk = (int) value;
             cudaSetDevice(device);
             FA2_TRY(cudaStreamSynchronize(s), "the computation on the GPU failed", 1);

@@ -251,8 +251,9 @@ def test_fixed_nodes(gpu, golden):
 @pytest.mark.parametrize("prec", ["single", "double"])
 @pytest.mark.parametrize("adjust", [False, True])
 def test_warp_walk_equals_thread_walk(gpu, prec, adjust):
-    """The warp-synchronous walk keeps every lane's own decisions: its forces
-    are those of one independent walk per thread."""
+    """The warp-synchronous walk and the walks of two or four nodes per
+    thread keep every node's own decisions: their forces are those of one
+    independent walk per thread."""
     n, a, b = G.barabasi_albert(30000, 3, seed=4)
     w = np.random.default_rng(2).lognormal(0.0, 0.5, len(a))
     pos = f32(G.uniform_positions(n, -2000, 2000, seed=5))
@@ -269,8 +270,14 @@ def test_warp_walk_equals_thread_walk(gpu, prec, adjust):
         fw2 = L.forces(pos)
         L.option("walk", 2)
         fwide = L.forces(pos)
+        L.option("walk", 3)
+        fpair = L.forces(pos)
+        L.option("walk", 4)
+        fquad = L.forces(pos)
     np.testing.assert_array_equal(ft, ft2)
     np.testing.assert_array_equal(ft, fwide)
+    np.testing.assert_array_equal(ft, fpair)  # two nodes per thread
+    np.testing.assert_array_equal(ft, fquad)  # four nodes per thread
     np.testing.assert_array_equal(fw, fw2)
     if prec == "double":
         np.testing.assert_array_equal(fw, ft)
