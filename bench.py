@@ -219,7 +219,8 @@ def run_exact(args):
     pairs = float(n) * n
     tflops = 20.0 * pairs / (ms / 1000.0) / 1e12
     print(json.dumps({"workload": f"exact all-pairs repulsion, n={n}, FP32",
-                      "kernel": "k_exact<float, 0, 2>", "launch_ms": ms,
+                      "kernel": "k_exact<float, 0, 4> (+ k_pack, k_exact_sum)",
+                      "launch_ms": ms,
                       "pairs_per_s": pairs / (ms / 1000.0),
                       "fp32_tflops_20flop_convention": tflops,
                       "n": n}), flush=True)

@@ -75,6 +75,7 @@ def load(build_if_missing: bool = False):
         "fa2cu_batch_positions": (C.c_int, [C.c_void_p, C.c_int, P_D]),
         "fa2cu_batch_speed": (C.c_int, [C.c_void_p, C.c_int, P_D]),
         "fa2cu_batch_stream": (C.c_void_p, [C.c_void_p]),
+        "fa2cu_batch_phase_cycles": (C.c_int, [C.c_void_p, C.c_int, P_D]),
         "fa2cu_batch_bytes": (C.c_double, [C.c_void_p]),
         "fa2cu_batch_close": (None, [C.c_void_p]),
         "fa2cu_batch_tune": (C.c_int, [C.c_int, C.c_int, P_I, P_I]),
@@ -123,6 +124,7 @@ EXPORTED = (
     "fa2cu_layout_close", "fa2cu_build_info", "fa2cu_morton_order_noalloc",
     "fa2cu_batch_open", "fa2cu_batch_iterate", "fa2cu_batch_sync",
     "fa2cu_batch_positions", "fa2cu_batch_speed", "fa2cu_batch_stream",
+    "fa2cu_batch_phase_cycles",
     "fa2cu_batch_bytes", "fa2cu_batch_close", "fa2cu_batch_tune",
     "fa2cu_server_open", "fa2cu_server_submit", "fa2cu_server_wait",
     "fa2cu_server_collect",

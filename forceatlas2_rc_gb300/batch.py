@@ -116,6 +116,16 @@ class Batch:
         return dict(speed=st[0], efficiency=st[1], total_swinging=st[2],
                     total_traction=st[3])
 
+    PHASES = ("codes", "sort", "tree", "sums", "repulsion", "attraction",
+              "totals", "move")
+
+    def phase_cycles(self, iterations: int = 1) -> dict:
+        """SM cycles per phase, summed over the blocks, of `iterations`
+        instrumented iterations (the positions advance)."""
+        c = np.zeros(8)
+        self._check(self.lib.fa2cu_batch_phase_cycles(self.h, int(iterations), dptr(c)))
+        return dict(zip(self.PHASES, c))
+
     @property
     def stream(self) -> int:
         return self.lib.fa2cu_batch_stream(self.h) or 0

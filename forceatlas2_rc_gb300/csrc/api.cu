@@ -435,6 +435,14 @@ int fa2cu_batch_sync(fa2cu_batch *B) { return B->impl->sync(); }
 int fa2cu_batch_positions(fa2cu_batch *B, int g, double *pos) { return B->impl->positions(g, pos); }
 int fa2cu_batch_speed(fa2cu_batch *B, int g, double state[4]) { return B->impl->speed(g, state); }
 void *fa2cu_batch_stream(fa2cu_batch *B) { return (void *) B->impl->stream(); }
+int fa2cu_batch_phase_cycles(fa2cu_batch *B, int iterations, double cycles[8])
+{
+    if (iterations < 1) {
+        set_message("invalid number of iterations");
+        return 1;
+    }
+    return B->impl->phase_cycles(iterations, cycles);
+}
 double fa2cu_batch_bytes(const fa2cu_batch *B) { return B->impl->bytes(); }
 void fa2cu_batch_close(fa2cu_batch *B)
 {

@@ -65,7 +65,13 @@ template <class R> struct BatchArrays {
     int *parent, *rope, *visits;
     Agg<R> *agg;
     BHNode<R> *nodes;
+    // per block, the cycles spent in each of the 8 phases of an iteration
+    // (measurement launches only; nullptr otherwise)
+    unsigned long long *prof;
 };
+
+// Phases of a batched iteration, as counted in BatchArrays::prof.
+enum { BP_CODES, BP_SORT, BP_TREE, BP_SUMS, BP_REPULSION, BP_ATTRACTION, BP_TOTALS, BP_MOVE };
 
 // ---- block-level building blocks ----------------------------------------------
 
@@ -241,8 +247,18 @@ k_batch(int ngraphs, BatchGraph *graphs, const int *queue, int *next, int iterat
         }
         double speed = G->speed, eff = G->efficiency;
 
+        // phase clock of thread 0, read after each block-wide barrier
+        long long tlast = clock64();
+        auto phase = [&](int ph) {
+            if (A.prof && tid == 0) {
+                const long long t = clock64();
+                A.prof[(size_t) blockIdx.x * 8 + ph] += (unsigned long long) (t - tlast);
+                tlast = t;
+            }
+        };
         for (int it = 0; it < iterations; it++) {
             __syncthreads();
+            phase(BP_MOVE);
             if (sh_stop) break;
             if (exact || n < 2) {
                 // records in original order; the all-pairs sum per node over
@@ -252,43 +268,71 @@ k_batch(int ngraphs, BatchGraph *graphs, const int *queue, int *next, int iterat
                     psort[i] = mk4<R>(p.x, p.y, mass[i], adjust ? size[i] : R(0));
                 }
                 R4 *tile = reinterpret_cast<R4 *>(&cnt[0][0]);
-                for (int i0 = 0; i0 < n; i0 += T) {
-                    const int i = i0 + tid;
-                    const R4 me = i < n ? psort[i] : mk4<R>(R(0), R(0), R(0), R(0));
-                    R ax = R(0), ay = R(0);
-                    const float smi = (float) scaling * (float) me.z;
+                // two nodes per thread (i and i + T): each tile record feeds
+                // two independent sums; every node still sums j ascending
+                for (int i0 = 0; i0 < n; i0 += 2 * T) {
+                    const int ia = i0 + tid, ib = ia + T;
+                    const R4 zero = mk4<R>(R(0), R(0), R(0), R(0));
+                    const R4 ma = ia < n ? psort[ia] : zero, mb = ib < n ? psort[ib] : zero;
+                    R axa = R(0), aya = R(0), axb = R(0), ayb = R(0);
+                    const float smia = (float) scaling * (float) ma.z;
+                    const float smib = (float) scaling * (float) mb.z;
                     for (int j0 = 0; j0 < n; j0 += T) {
                         __syncthreads();
                         if (j0 + tid < n) tile[tid] = psort[j0 + tid];
                         __syncthreads();
                         const int m = min(T, n - j0);
                         if (sizeof(R) == 4 && !adjust) {
+#pragma unroll 4
                             for (int jj = 0; jj < m; jj++) {
                                 const R4 q = tile[jj];
-                                const float xd = (float) me.x - (float) q.x;
-                                const float yd = (float) me.y - (float) q.y;
-                                const float d2 = fmaf(xd, xd, yd * yd);
-                                const float r = __fdividef(1.0f, d2);
-                                const float g = d2 > 0.0f ? smi * (float) q.z * r : 0.0f;
-                                ax = (R) fmaf(xd, g, (float) ax);
-                                ay = (R) fmaf(yd, g, (float) ay);
+                                const float xda = (float) ma.x - (float) q.x;
+                                const float yda = (float) ma.y - (float) q.y;
+                                const float xdb = (float) mb.x - (float) q.x;
+                                const float ydb = (float) mb.y - (float) q.y;
+                                const float d2a = fmaf(xda, xda, yda * yda);
+                                const float d2b = fmaf(xdb, xdb, ydb * ydb);
+                                const float ga =
+                                    d2a > 0.0f ? (float) q.z * __fdividef(1.0f, d2a) : 0.0f;
+                                const float gb =
+                                    d2b > 0.0f ? (float) q.z * __fdividef(1.0f, d2b) : 0.0f;
+                                axa = (R) fmaf(xda, ga, (float) axa);
+                                aya = (R) fmaf(yda, ga, (float) aya);
+                                axb = (R) fmaf(xdb, gb, (float) axb);
+                                ayb = (R) fmaf(ydb, gb, (float) ayb);
                             }
                         } else {
                             for (int jj = 0; jj < m; jj++) {
                                 const R4 q = tile[jj];
-                                const R xd = me.x - q.x, yd = me.y - q.y;
-                                const R g = adjust ? rep_factor<R, true>(xd * xd + yd * yd,
-                                                                         me.z * q.z, me.w + q.w,
-                                                                         scaling)
-                                                   : rep_factor<R, false>(xd * xd + yd * yd,
-                                                                          me.z * q.z, R(0),
-                                                                          scaling);
-                                ax += xd * g;
-                                ay += yd * g;
+                                const R xda = ma.x - q.x, yda = ma.y - q.y;
+                                const R xdb = mb.x - q.x, ydb = mb.y - q.y;
+                                R ga, gb;
+                                if (adjust) {
+                                    ga = rep_factor<R, true>(xda * xda + yda * yda, ma.z * q.z,
+                                                             ma.w + q.w, scaling);
+                                    gb = rep_factor<R, true>(xdb * xdb + ydb * ydb, mb.z * q.z,
+                                                             mb.w + q.w, scaling);
+                                } else {
+                                    ga = rep_factor<R, false>(xda * xda + yda * yda, ma.z * q.z,
+                                                              R(0), scaling);
+                                    gb = rep_factor<R, false>(xdb * xdb + ydb * ydb, mb.z * q.z,
+                                                              R(0), scaling);
+                                }
+                                axa += xda * ga;
+                                aya += yda * ga;
+                                axb += xdb * gb;
+                                ayb += ydb * gb;
                             }
                         }
                     }
-                    if (i < n) f[i] = mk2<R>(ax, ay);
+                    if (sizeof(R) == 4 && !adjust) { // scaling * m_i, once
+                        axa = (R) ((float) axa * smia);
+                        aya = (R) ((float) aya * smia);
+                        axb = (R) ((float) axb * smib);
+                        ayb = (R) ((float) ayb * smib);
+                    }
+                    if (ia < n) f[ia] = mk2<R>(axa, aya);
+                    if (ib < n) f[ib] = mk2<R>(axb, ayb);
                 }
             } else {
                 // bounding box and the Morton quantisation
@@ -340,7 +384,9 @@ k_batch(int ngraphs, BatchGraph *graphs, const int *queue, int *next, int iterat
                     idx[i] = (uint32_t) i;
                 }
                 __syncthreads();
+                phase(BP_CODES);
                 block_sort_pairs<W>(n, key, idx, kb, vb, cnt, dbase);
+                phase(BP_SORT);
                 for (int k = tid; k < n; k += T) {
                     const uint32_t i = idx[k];
                     const R2 p = pos[i];
@@ -349,10 +395,12 @@ k_batch(int ngraphs, BatchGraph *graphs, const int *queue, int *next, int iterat
                 for (int i = tid; i < n - 1; i += T)
                     karras_one<false>(i, n, key, child, range, parent, rope, visits);
                 __syncthreads();
+                phase(BP_TREE);
                 for (int k = tid; k < n; k += T)
                     climb<R, true>(k, n, psort, child, parent, range, rope, visits, agg, nodes,
                                    status);
                 __syncthreads();
+                phase(BP_SUMS);
                 for (int k = tid; k < n; k += T) {
                     const R2 fk =
                         adjust ? walk<R, true>(k, n, scaling, theta2, theta2d, psort, nodes,
@@ -363,10 +411,12 @@ k_batch(int ngraphs, BatchGraph *graphs, const int *queue, int *next, int iterat
                 }
             }
             __syncthreads();
+            phase(BP_REPULSION);
             for (int i = tid; i < n; i += T)
                 attract_one<R>(i, gravity, strong, linlog, adjust, pos, mass, size, off, A.inc,
                                f);
             __syncthreads();
+            phase(BP_ATTRACTION);
             // swinging and traction; totals in double in a fixed order: in
             // FP64 up to SERIAL_TOTALS_MAX nodes serially in node order (the
             // reference's order, as the single-graph path), else per thread
@@ -420,6 +470,7 @@ k_batch(int ngraphs, BatchGraph *graphs, const int *queue, int *next, int iterat
                 }
             }
             __syncthreads();
+            phase(BP_TOTALS);
             if (sh_stop) break;
             const R sp = (R) sh_speed;
             for (int i = tid; i < n; i += T) {
@@ -667,6 +718,46 @@ template <class R> struct Batch : BatchBase {
         execs.clear();
     }
 
+    // Cycles of each phase, summed over the blocks, over `iterations`
+    // iterations of every graph (an uncaptured, instrumented launch).
+    int phase_cycles(int iterations, double out[8]) override
+    {
+        cudaSetDevice(device);
+        DevMem tmp;
+        unsigned long long *prof = tmp.get<unsigned long long>((size_t) blocks * 8);
+        if (tmp.failed) {
+            set_cuda_error("could not allocate memory on the device", tmp.err);
+            return 1;
+        }
+        int rc = cudaMemsetAsync(prof, 0, (size_t) blocks * 8 * sizeof(unsigned long long), s) !=
+                 cudaSuccess;
+        BatchArrays<R> P = A;
+        P.prof = prof;
+        if (!rc) rc = cudaMemsetAsync(next, 0, sizeof(int), s) != cudaSuccess;
+        if (!rc) {
+            if (threads == 256)
+                k_batch<R, 256><<<blocks, 256, 0, s>>>(G, graphs, queue, next, iterations, P,
+                                                       status);
+            else
+                k_batch<R, 512><<<blocks, 512, 0, s>>>(G, graphs, queue, next, iterations, P,
+                                                       status);
+        }
+        std::vector<unsigned long long> h((size_t) blocks * 8);
+        if (!rc)
+            rc = cudaMemcpyAsync(h.data(), prof, h.size() * sizeof(unsigned long long),
+                                 cudaMemcpyDeviceToHost, s) != cudaSuccess;
+        if (!rc) rc = cudaStreamSynchronize(s) != cudaSuccess;
+        tmp.release();
+        if (rc) {
+            set_message("the computation on the GPU failed");
+            return 1;
+        }
+        for (int k = 0; k < 8; k++) out[k] = 0.0;
+        for (size_t b = 0; b < (size_t) blocks; b++)
+            for (int k = 0; k < 8; k++) out[k] += (double) h[b * 8 + k];
+        return 0;
+    }
+
     int sync() override
     {
         cudaSetDevice(device);
@@ -739,10 +830,11 @@ BatchBase *make_batch(const fa2_full_params *ps, int count, const double *const 
 
 // ---- autotuner -------------------------------------------------------------------
 // The exact-vs-Barnes-Hut crossover and the block size, measured on the
-// device: Erdos-Renyi graphs (mean degree 8) of 64 .. 4096 nodes, two per SM,
-// laid out for 2 iterations (after 2) in each mode; the crossover is the
-// smallest size at which the tree is faster. Block sizes 256 and 512 are
-// compared on 2048-node graphs.
+// device: Erdos-Renyi graphs (mean degree 8), two per SM, laid out for 2
+// iterations (after 2) in each mode, at 64, 128, .. 16384 nodes until the
+// tree is faster, then at quarter-octave sizes below that one; the crossover
+// is the smallest size measured at which the tree is faster. Block sizes 256
+// and 512 are compared on 2048-node graphs.
 
 struct TuneGraphs {
     std::vector<std::vector<int>> off, node;
@@ -848,16 +940,36 @@ template <class R> int tune_batch(int device, int *exact_below, int *threads)
     FA2_TRY(cudaSetDevice(device), "could not use the CUDA device", 1);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
     const int copies = 2 * std::max(sms, 1);
-    int cross = 8192;
-    for (int n = 64; n <= 4096; n *= 2) {
+    // 1: tree faster, 0: exact faster, -1: error
+    auto tree_wins = [&](int n) {
         TuneGraphs t;
         tune_graphs(t, n, copies, device, sizeof(R) == 8);
         const double te = time_batch<R>(t, 1 << 30, 512);
         const double tb = time_batch<R>(t, 0, 512);
-        if (te < 0 || tb < 0) return 1;
-        if (tb < te) {
-            cross = n;
+        if (te < 0 || tb < 0) return -1;
+        return tb < te ? 1 : 0;
+    };
+    // the first power of two at which the tree wins, then quarter-octave
+    // steps below it
+    int hi = 0;
+    for (int n = 64; n <= 16384; n *= 2) {
+        const int w = tree_wins(n);
+        if (w < 0) return 1;
+        if (w) {
+            hi = n;
             break;
+        }
+    }
+    int cross = hi ? hi : 32768;
+    if (hi > 64) {
+        for (int q = 1; q < 4; q++) {
+            const int n = (int) std::lround((hi / 2) * std::pow(2.0, q / 4.0));
+            const int w = tree_wins(n);
+            if (w < 0) return 1;
+            if (w) {
+                cross = n;
+                break;
+            }
         }
     }
     TuneGraphs t;

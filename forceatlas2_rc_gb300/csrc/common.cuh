@@ -26,7 +26,13 @@ void set_cuda_error(const char *what, cudaError_t e);
 // Barnes-Hut walk variants (all give identical forces): warp-synchronous;
 // one walk per thread at 6 blocks of 256 per SM (<= 40 registers); one walk
 // per thread with the registers the compiler wants.
-enum { WALK_WARP = 0, WALK_THREAD = 1, WALK_THREAD_WIDE = 2, WALK_PAIR = 3, WALK_QUAD = 4 };
+enum {
+    WALK_WARP = 0,
+    WALK_THREAD = 1,
+    WALK_THREAD_WIDE = 2,
+    WALK_PAIR = 3,
+    WALK_QUAD = 4,
+};
 
 // Device-side status words (one int each in a session's `status` buffer).
 enum {

@@ -11,9 +11,9 @@ LayoutBase *make_layout_f64(const fa2_full_params *p, const double *pos, int rep
 {
     return make_layout<double>(p, pos, rep, opts, edges);
 }
-double layout_footprint_f64(int n, int ninc, int adjust, int any_fixed, int rep)
+double layout_footprint_f64(int n, int ninc, int adjust, int any_fixed, int rep, int sms)
 {
-    return layout_footprint<double>(n, ninc, adjust, any_fixed, rep);
+    return layout_footprint<double>(n, ninc, adjust, any_fixed, rep, sms);
 }
 RepulseBase *make_repulse_f64(int device, int n, int adjust, int bh)
 {

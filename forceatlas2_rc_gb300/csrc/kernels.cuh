@@ -419,7 +419,9 @@ __device__ __forceinline__ void climb(int k, int n, const typename RT<R>::R4 *ps
         const int2 rg = range[r];
         BHNode<R> nd;
         nd.c = agg_record(q);
-        nd.t = make_int4(c.x, rope[rg.y], rg.x, rg.y);
+        // a region of at most 8 nodes is never opened: its left link
+        // carries ~first instead, so that the walk tells it by the sign
+        nd.t = make_int4(rg.y - rg.x >= 8 ? c.x : ~rg.x, rope[rg.y], rg.x, rg.y);
         nodes[r] = nd;
         r = parent[r];
     }
@@ -489,15 +491,14 @@ walk(int k, int n, R scaling, R theta2, double theta2d,
     const R xi = me.x, yi = me.y, mi = me.z, si = me.w;
     R ax = R(0), ay = R(0);
     const int nl = n - 1;
+    // walk positions: regions 0 .. nl-1, single nodes nl .. nl+n-1; the walk
+    // ends at -1
+    const unsigned nend = (unsigned) (nl + n);
     int cur = 0, j = 0, jend = -1;
     // a walk visits each of the 2n-1 tree nodes and each node pair at most
-    // once: more steps than that, or an index out of range, is a bug
-    const int cap = 4 * n + 64;
+    // once: more steps than that, or a link out of range, is a bug
+    const int cap = 2 * n + 64;
     for (int step = 0;; step++) {
-        if (step > cap || cur >= nl + n || jend >= n) {
-            atomicOr(status + ST_ERROR, ERR_BOUNDS);
-            break;
-        }
         if (j <= jend) {
             if (j != k) {
                 const R4 q = psort[j];
@@ -510,7 +511,10 @@ walk(int k, int n, R scaling, R theta2, double theta2d,
             ++j;
             continue;
         }
-        if (cur < 0) break;
+        if ((unsigned) cur >= nend || step > cap) {
+            if (cur != -1) atomicOr(status + ST_ERROR, ERR_BOUNDS);
+            break;
+        }
         if (cur >= nl) { // a single node
             j = jend = cur - nl;
             cur = rope[j];
@@ -528,11 +532,15 @@ walk(int k, int n, R scaling, R theta2, double theta2d,
             ax += xd * g;
             ay += yd * g;
             cur = nd.t.y;
-        } else if (nd.t.w - nd.t.z >= 8) {
+        } else if (nd.t.x >= 0) {
             cur = nd.t.x;
-        } else {
+        } else { // at most 8 nodes: node by node
             j = nd.t.z;
             jend = nd.t.w;
+            if (j < 0 || jend >= n) {
+                atomicOr(status + ST_ERROR, ERR_BOUNDS);
+                break;
+            }
             cur = nd.t.y;
         }
     }
@@ -641,7 +649,7 @@ walk_multi(int k0, int cnt, int n, R scaling, R theta2, double theta2d,
         }
         if (nearm == 0) {
             cur = nd.t.y;
-        } else if (nd.t.w - nd.t.z >= 8) {
+        } else if (nd.t.x >= 0) {
             cur = nd.t.x;
         } else {
             j = nd.t.z;
@@ -731,7 +739,7 @@ k_traverse_warp(int n, R scaling, R theta2, double theta2d,
                 ax += xd * g;
                 ay += yd * g;
                 resume = nd.t.w + 1;
-            } else if (nd.t.w - nd.t.z >= 8) {
+            } else if (nd.t.x >= 0) {
                 open = true;
             } else {
                 direct = true;
@@ -785,7 +793,7 @@ k_traverse_count(int n, R theta2, double theta2d, const typename RT<R>::R4 *__re
                 far = far_dd(agg + cur, (float) me.x, (float) me.y, theta2d);
             if (far) {
                 cur = nd.t.y;
-            } else if (nd.t.w - nd.t.z >= 8) {
+            } else if (nd.t.x >= 0) {
                 cur = nd.t.x;
             } else {
                 pairs += nd.t.w - nd.t.z + 1 - (k >= nd.t.z && k <= nd.t.w);
@@ -1171,7 +1179,16 @@ k_forces_out(int n, const typename RT<R>::R2 *__restrict__ f, const int *__restr
 // test is needed. Every mbarrier wait is bounded in time: on expiry the
 // kernel records ERR_WAIT, drains its copies in flight and returns.
 
-#define FA2_EXACT_THREADS 128
+#define FA2_EXACT_THREADS 256
+#ifndef FA2_EXACT_IPT_F32
+#define FA2_EXACT_IPT_F32 4 // nodes per thread in FP32 (FP64: 1)
+#endif
+
+// Records per tile of the all-pairs kernel (8 KB of records, double-buffered).
+template <class R> __host__ __device__ constexpr int exact_tile()
+{
+    return 8192 / (int) sizeof(typename RT<R>::R4);
+}
 
 __device__ __forceinline__ uint32_t smem_addr(const void *p)
 {
@@ -1229,13 +1246,18 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, unsigned phase,
     }
 }
 
+// Block (x, y) sums, for its FA2_EXACT_THREADS * IPT nodes, the sources
+// [y seg, min(n, (y + 1) seg)) (seg a multiple of the tile): into f when the
+// grid has one row (every j, ascending: the reference's order), else into
+// row y of `partial` (n entries per row), summed by k_exact_sum.
 template <class R, bool ADJUST, int IPT>
 __global__ void __launch_bounds__(FA2_EXACT_THREADS)
 k_exact(int n, R scaling, const typename RT<R>::R4 *__restrict__ nodes,
-        typename RT<R>::R2 *__restrict__ f, int *__restrict__ status)
+        typename RT<R>::R2 *__restrict__ f, typename RT<R>::R2 *__restrict__ partial, int seg,
+        int *__restrict__ status)
 {
     typedef typename RT<R>::R4 R4;
-    constexpr int TILE = 32768 / sizeof(R4); // records per 32 KB tile
+    constexpr int TILE = exact_tile<R>();
     extern __shared__ __align__(128) unsigned char smem[];
     R4 *tile = reinterpret_cast<R4 *>(smem);
     uint64_t *bar = reinterpret_cast<uint64_t *>(smem + 2 * TILE * sizeof(R4));
@@ -1254,7 +1276,9 @@ k_exact(int n, R scaling, const typename RT<R>::R4 *__restrict__ nodes,
         smi[u] = scaling * p.z;
         ax[u] = ay[u] = R(0);
     }
-    const int ntiles = (n + TILE - 1) / TILE;
+    const int j0 = blockIdx.y * seg, j1 = min(n, j0 + seg);
+    const R4 *src = nodes + j0;
+    const int ntiles = (j1 - j0 + TILE - 1) / TILE;
     if (threadIdx.x == 0) {
         failed = 0;
         mbar_init(&bar[0], 1);
@@ -1265,8 +1289,8 @@ k_exact(int n, R scaling, const typename RT<R>::R4 *__restrict__ nodes,
     __syncthreads();
     if (threadIdx.x == 0) {
         for (int t = 0; t < 2 && t < ntiles; t++) {
-            const int cnt = min(TILE, n - t * TILE);
-            tma_load_1d(tile + t * TILE, nodes + (size_t) t * TILE, cnt * (unsigned) sizeof(R4),
+            const int cnt = min(TILE, j1 - j0 - t * TILE);
+            tma_load_1d(tile + t * TILE, src + (size_t) t * TILE, cnt * (unsigned) sizeof(R4),
                         &bar[t]);
         }
     }
@@ -1285,10 +1309,15 @@ k_exact(int n, R scaling, const typename RT<R>::R4 *__restrict__ nodes,
             return;
         }
         const R4 *q = tile + b * TILE;
-        const int cnt = min(TILE, n - t * TILE);
+        const int cnt = min(TILE, j1 - j0 - t * TILE);
         if constexpr (sizeof(R) == 4 && !ADJUST) {
-            // FP32: 9 FP32-pipe operations and one MUFU reciprocal per pair,
-            // with the thread's scaling * m_i hoisted out of the loop
+            // FP32: 7 FP32-pipe operations, one min and one MUFU reciprocal
+            // per pair; the thread's scaling * m_i multiplies the sums once
+            // at the end. A coincident pair (xd = yd = 0, d2 = 0) has an
+            // infinite reciprocal: capping g at FLT_MAX makes its term 0,
+            // the reference's factor for d2 = 0. (d2 is also 0 when both
+            // offsets are below 1e-19, whose squares flush to zero; such a
+            // pair has no meaningful float force either way.)
 #pragma unroll 4
             for (int jj = 0; jj < cnt; jj++) {
                 const R4 p = q[jj];
@@ -1296,8 +1325,7 @@ k_exact(int n, R scaling, const typename RT<R>::R4 *__restrict__ nodes,
                 for (int u = 0; u < IPT; u++) {
                     const float xd = xi[u] - p.x, yd = yi[u] - p.y;
                     const float d2 = fmaf(xd, xd, yd * yd);
-                    const float r = __fdividef(1.0f, d2);
-                    const float g = d2 > 0.0f ? smi[u] * p.z * r : 0.0f;
+                    const float g = fminf(p.z * __fdividef(1.0f, d2), 3.402823466e38f);
                     ax[u] = fmaf(xd, g, ax[u]);
                     ay[u] = fmaf(yd, g, ay[u]);
                 }
@@ -1319,22 +1347,64 @@ k_exact(int n, R scaling, const typename RT<R>::R4 *__restrict__ nodes,
         __syncthreads(); // every thread is done with buffer b
         if (threadIdx.x == 0 && t + 2 < ntiles) {
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-            const int cnt2 = min(TILE, n - (t + 2) * TILE);
-            tma_load_1d(tile + b * TILE, nodes + (size_t) (t + 2) * TILE,
+            const int cnt2 = min(TILE, j1 - j0 - (t + 2) * TILE);
+            tma_load_1d(tile + b * TILE, src + (size_t) (t + 2) * TILE,
                         cnt2 * (unsigned) sizeof(R4), &bar[b]);
         }
     }
 #pragma unroll
     for (int u = 0; u < IPT; u++) {
         const int i = i0 + u * FA2_EXACT_THREADS;
-        if (i < n) f[i] = mk2<R>(ax[u], ay[u]);
+        if (sizeof(R) == 4 && !ADJUST) {
+            ax[u] *= smi[u];
+            ay[u] *= smi[u];
+        }
+        if (i < n) {
+            if (partial)
+                partial[(size_t) blockIdx.y * n + i] = mk2<R>(ax[u], ay[u]);
+            else
+                f[i] = mk2<R>(ax[u], ay[u]);
+        }
     }
+}
+
+// The rows of k_exact's partial sums, in row order.
+template <class R>
+__global__ void __launch_bounds__(256)
+k_exact_sum(int n, int rows, const typename RT<R>::R2 *__restrict__ partial,
+            typename RT<R>::R2 *__restrict__ f)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    typename RT<R>::R2 a = partial[i];
+    for (int r = 1; r < rows; r++) {
+        const typename RT<R>::R2 b = partial[(size_t) r * n + i];
+        a.x += b.x;
+        a.y += b.y;
+    }
+    f[i] = a;
 }
 
 template <class R> constexpr size_t exact_smem_bytes()
 {
-    return 2 * 32768 + 2 * sizeof(uint64_t);
+    return 2 * (size_t) exact_tile<R>() * sizeof(typename RT<R>::R4) + 2 * sizeof(uint64_t);
 }
+
+// Rows of source ranges for an n-node all-pairs sum on a GPU of `sms` SMs:
+// enough blocks for about six per SM, each range at least two tiles long;
+// 1 in double (every node sums every j in order) or when n alone fills the
+// GPU.
+template <class R> int exact_rows(int n, int sms, int ipt)
+{
+    if (sizeof(R) != 4) return 1;
+    const int nb = (n + FA2_EXACT_THREADS * ipt - 1) / (FA2_EXACT_THREADS * ipt);
+    const int want = (6 * sms + nb - 1) / nb;
+    const int most = n / (2 * exact_tile<R>());
+    int rows = want < most ? want : most;
+    if (rows > 16) rows = 16;
+    return rows < 1 ? 1 : rows;
+}
+
 
 // ---- quadtree traversal of fa2_gpu_repulse_bh (reference src/gpu.c:78-123)
 // Regions of the host's Gephi quadtree, converted on the device.

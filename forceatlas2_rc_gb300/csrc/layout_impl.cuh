@@ -37,6 +37,28 @@ inline double now_s()
 }
 
 // Device allocations of a session, released together.
+// The all-pairs repulsion of n packed records into f: k_exact over `rows`
+// source ranges (exact_rows), then their fixed-order sum when rows > 1
+// (partial holds rows * n entries).
+template <class R, int IPT>
+void launch_exact(cudaStream_t s, int n, bool adjust, R scaling, const typename RT<R>::R4 *packed,
+                  typename RT<R>::R2 *f, typename RT<R>::R2 *partial, int rows, int *status)
+{
+    constexpr int TILE = exact_tile<R>();
+    const int seg = rows > 1 ? ceil_div(ceil_div(n, rows), TILE) * TILE : ceil_div(n, TILE) * TILE;
+    rows = ceil_div(n, seg);
+    const dim3 grid(ceil_div(n, FA2_EXACT_THREADS * IPT), rows);
+    const size_t smem = exact_smem_bytes<R>();
+    typename RT<R>::R2 *part = rows > 1 ? partial : nullptr;
+    if (adjust)
+        k_exact<R, true, IPT><<<grid, FA2_EXACT_THREADS, smem, s>>>(n, scaling, packed, f, part,
+                                                                    seg, status);
+    else
+        k_exact<R, false, IPT><<<grid, FA2_EXACT_THREADS, smem, s>>>(n, scaling, packed, f, part,
+                                                                     seg, status);
+    if (rows > 1) k_exact_sum<R><<<ceil_div(n, 256), 256, 0, s>>>(n, rows, partial, f);
+}
+
 template <class R> struct Layout : LayoutBase {
     typedef typename RT<R>::R2 R2;
     typedef typename RT<R>::R4 R4;
@@ -59,6 +81,8 @@ template <class R> struct Layout : LayoutBase {
     uint32_t *key = nullptr, *order = nullptr;
     SortScratch ss{};
     R4 *psort = nullptr, *packed = nullptr;
+    R2 *exact_part = nullptr; // exact_rows rows of partial sums (rows > 1)
+    int exact_nrows = 1;
     int2 *child = nullptr, *range = nullptr;
     int *parent = nullptr, *rope = nullptr, *visits = nullptr;
     Agg<R> *agg = nullptr;
@@ -125,6 +149,7 @@ template <class R> struct Layout : LayoutBase {
             nodes = mem.get<BHNode<R>>(nn - 1);
         } else {
             packed = mem.get<R4>(nn);
+            if (exact_nrows > 1) exact_part = mem.get<R2>((size_t) exact_nrows * nn);
         }
         if (mem.failed) {
             set_cuda_error("could not allocate memory on the device", mem.err);
@@ -221,6 +246,11 @@ template <class R> struct Layout : LayoutBase {
         for (auto &e : ev) FA2_TRY(cudaEventCreate(&e), "could not create a CUDA event", 1);
         mem.pool = opts ? opts->pool : nullptr;
         mem.s = s;
+        if (rep == FA2CU_REPULSION_EXACT) {
+            int sms = 0;
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+            exact_nrows = exact_rows<R>(n, std::max(sms, 1), EXACT_IPT);
+        }
         if (alloc(rep == FA2CU_REPULSION_BH)) return 1;
 
         // the graph, once (reference src/gpu_full.c:241-287), or prepared on
@@ -291,7 +321,7 @@ template <class R> struct Layout : LayoutBase {
         return 0;
     }
 
-    static constexpr int EXACT_IPT = sizeof(R) == 4 ? 2 : 1;
+    static constexpr int EXACT_IPT = sizeof(R) == 4 ? FA2_EXACT_IPT_F32 : 1;
 
     // ---- the steps of one iteration ----
     void launch_build()
@@ -352,14 +382,8 @@ template <class R> struct Layout : LayoutBase {
             }
         } else {
             k_pack<R><<<ceil_div(n, 256), 256, 0, s>>>(n, adjust, pos, mass, size, packed);
-            const int grid = ceil_div(n, FA2_EXACT_THREADS * EXACT_IPT);
-            const size_t smem = exact_smem_bytes<R>();
-            if (adjust)
-                k_exact<R, true, EXACT_IPT><<<grid, FA2_EXACT_THREADS, smem, s>>>(
-                    n, scaling, packed, f, status);
-            else
-                k_exact<R, false, EXACT_IPT><<<grid, FA2_EXACT_THREADS, smem, s>>>(
-                    n, scaling, packed, f, status);
+            launch_exact<R, EXACT_IPT>(s, n, adjust, scaling, packed, f, exact_part, exact_nrows,
+                                       status);
         }
     }
     void launch_attraction()
@@ -614,13 +638,16 @@ LayoutBase *make_layout(const fa2_full_params *p, const double *pos, int rep,
 
 // Device bytes a layout holds (its buffers, counted by the allocation plan
 // itself) plus the transient staging of the graph upload at open.
-template <class R> double layout_footprint(int n, int ninc, int adjust, int any_fixed, int rep)
+template <class R>
+double layout_footprint(int n, int ninc, int adjust, int any_fixed, int rep, int sms)
 {
     Layout<R> L;
     L.n = n;
     L.ninc = ninc;
     L.adjust = adjust ? 1 : 0;
     L.any_fixed = any_fixed ? 1 : 0;
+    if (rep == FA2CU_REPULSION_EXACT)
+        L.exact_nrows = exact_rows<R>(n, std::max(sms, 1), Layout<R>::EXACT_IPT);
     L.mem.dry = true;
     L.alloc(rep == FA2CU_REPULSION_BH);
     const double staging = (double) std::max(n, ninc) * sizeof(double) + (double) ninc * sizeof(int);
@@ -640,6 +667,8 @@ template <class R> struct Repulse : RepulseBase {
     double *host2 = nullptr; // pinned copy of out2
     R4 *p = nullptr;
     R2 *f = nullptr;
+    R2 *part = nullptr; // partial sums of the split all-pairs kernel
+    int nrows = 1;
     int *status = nullptr;
     fa2_region *raw = nullptr;
     QRegion<R> *regs = nullptr;
@@ -666,6 +695,12 @@ template <class R> struct Repulse : RepulseBase {
         p = mem.get<R4>(nn);
         f = mem.get<R2>(nn);
         status = mem.get<int>(ST_COUNT);
+        if (!barnes_hut) {
+            int sms = 0;
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+            nrows = exact_rows<R>(n, std::max(sms, 1), Layout<R>::EXACT_IPT);
+            if (nrows > 1) part = mem.get<R2>((size_t) nrows * nn);
+        }
         if (barnes_hut) {
             raw = mem.get<fa2_region>(2 * nn);
             regs = mem.get<QRegion<R>>(2 * nn);
@@ -743,15 +778,7 @@ template <class R> struct Repulse : RepulseBase {
         FA2_TRY(cudaStreamSynchronize(s), "the computation on the GPU failed", 1);
         double t1 = now_s();
         t_send += t1 - t0;
-        const int ipt = Layout<R>::EXACT_IPT;
-        const int grid = ceil_div(n, FA2_EXACT_THREADS * ipt);
-        const size_t smem = exact_smem_bytes<R>();
-        if (adjust)
-            k_exact<R, true, Layout<R>::EXACT_IPT><<<grid, FA2_EXACT_THREADS, smem, s>>>(
-                n, (R) sc, p, f, status);
-        else
-            k_exact<R, false, Layout<R>::EXACT_IPT><<<grid, FA2_EXACT_THREADS, smem, s>>>(
-                n, (R) sc, p, f, status);
+        launch_exact<R, Layout<R>::EXACT_IPT>(s, n, adjust, (R) sc, p, f, part, nrows, status);
         FA2_TRY(cudaGetLastError(), "the computation on the GPU failed", 1);
         FA2_TRY(cudaStreamSynchronize(s), "the computation on the GPU failed", 1);
         if (check_status()) return 1;

@@ -264,12 +264,30 @@ struct fa2cu_server {
 
 extern "C" {
 
+static int device_sms(int device)
+{
+    int sms = 0;
+    if (device < 0 && cudaGetDevice(&device) != cudaSuccess) return 1;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) {
+        cudaGetLastError();
+        return 1;
+    }
+    return sms > 0 ? sms : 1;
+}
+
+static double footprint_on(int device, int n, int ninc, int adjust, int any_fixed, int use_double,
+                           int repulsion)
+{
+    if (n < 1 || ninc < 0) return 0.0;
+    const int sms = device_sms(device);
+    return use_double ? layout_footprint_f64(n, ninc, adjust, any_fixed, repulsion, sms)
+                      : layout_footprint_f32(n, ninc, adjust, any_fixed, repulsion, sms);
+}
+
 double fa2cu_layout_footprint(int n, int ninc, int adjust, int any_fixed, int use_double,
                               int repulsion)
 {
-    if (n < 1 || ninc < 0) return 0.0;
-    return use_double ? layout_footprint_f64(n, ninc, adjust, any_fixed, repulsion)
-                      : layout_footprint_f32(n, ninc, adjust, any_fixed, repulsion);
+    return footprint_on(-1, n, ninc, adjust, any_fixed, use_double, repulsion);
 }
 
 fa2cu_server *fa2cu_server_open(const fa2cu_server_config *cfg)
@@ -351,8 +369,8 @@ long long fa2cu_server_submit(fa2cu_server *h, const fa2_full_params *p, const d
     int any_fixed = 0;
     if (p->fixed)
         for (int i = 0; i < n && !any_fixed; i++) any_fixed = p->fixed[i] != 0;
-    const double fp = fa2cu_layout_footprint(n, ninc, p->adjust, any_fixed, p->use_double,
-                                             repulsion);
+    const double fp =
+        footprint_on(S->device, n, ninc, p->adjust, any_fixed, p->use_double, repulsion);
     if (fp > S->budget) {
         set_message("the job needs %.0f bytes of device memory, more than the server's "
                     "budget of %.0f",

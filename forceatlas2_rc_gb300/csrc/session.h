@@ -54,9 +54,10 @@ LayoutBase *make_layout_f32(const fa2_full_params *p, const double *pos, int rep
                             const LayoutOpts *opts = nullptr, const EdgeList *edges = nullptr);
 LayoutBase *make_layout_f64(const fa2_full_params *p, const double *pos, int repulsion,
                             const LayoutOpts *opts = nullptr, const EdgeList *edges = nullptr);
-// Device bytes of a layout of n nodes and ninc incidences, staging included.
-double layout_footprint_f32(int n, int ninc, int adjust, int any_fixed, int repulsion);
-double layout_footprint_f64(int n, int ninc, int adjust, int any_fixed, int repulsion);
+// Device bytes of a layout of n nodes and ninc incidences, staging included,
+// on a device of `sms` SMs.
+double layout_footprint_f32(int n, int ninc, int adjust, int any_fixed, int repulsion, int sms);
+double layout_footprint_f64(int n, int ninc, int adjust, int any_fixed, int repulsion, int sms);
 
 struct RepulseBase {
     virtual ~RepulseBase() {}
@@ -80,6 +81,7 @@ struct BatchBase {
     virtual cudaStream_t stream() = 0;
     virtual double bytes() const = 0;
     virtual int count() const = 0;
+    virtual int phase_cycles(int iterations, double out[8]) = 0;
     int device = 0;
 };
 

@@ -143,12 +143,18 @@ int fa2cu_batch_positions(fa2cu_batch *B, int g, double *pos);
 /* Speed, efficiency and last swing / traction totals of graph g. */
 int fa2cu_batch_speed(fa2cu_batch *B, int g, double state[4]);
 void *fa2cu_batch_stream(fa2cu_batch *B);
+/* Run `iterations` iterations of every graph with a clock read after each
+ * phase (an uncaptured, instrumented launch) and return the SM cycles spent
+ * per phase, summed over the blocks: codes (bounding box, Morton), sort,
+ * tree (gather, Karras), sums (bottom-up), repulsion, attraction, totals
+ * (swing, traction, speed), move. */
+int fa2cu_batch_phase_cycles(fa2cu_batch *B, int iterations, double cycles[8]);
 double fa2cu_batch_bytes(const fa2cu_batch *B);
 void fa2cu_batch_close(fa2cu_batch *B);
 
 /* The autotuner: exact-vs-Barnes-Hut crossover (in nodes) and block size of
  * the batched engine, measured on `device` in the given precision (timed
- * batches of Erdos-Renyi graphs of 64 to 4096 nodes). Cached per device and
+ * batches of Erdos-Renyi graphs of 64 to 16384 nodes). Cached per device and
  * precision for the process. */
 int fa2cu_batch_tune(int device, int use_double, int *exact_below,
                      int *threads);
@@ -206,8 +212,9 @@ int fa2cu_server_stats(fa2cu_server *S, double out[8]);
 /* Stop the threads, drop the jobs not collected, release the pool. */
 void fa2cu_server_close(fa2cu_server *S);
 
-/* Device bytes a layout of n nodes and ninc incidences holds (its buffers
- * and the staging of the graph upload): the server's admission estimate. */
+/* Device bytes a layout of n nodes and ninc incidences holds on the current
+ * device (its buffers and the staging of the graph upload): the server's
+ * admission estimate. */
 double fa2cu_layout_footprint(int n, int ninc, int adjust, int any_fixed,
                               int use_double, int repulsion);
 

@@ -186,7 +186,7 @@ def test_batch_tune_and_errors(gpu):
     for prec in ("single", "double"):
         t = tune(0, prec)
         assert t["threads"] in (256, 512)
-        assert 64 <= t["exact_below"] <= 8192
+        assert 64 <= t["exact_below"] <= 32768
         assert tune(0, prec) == t
     g, pos = case(100, 1)
     with pytest.raises(RuntimeError, match="threads"):
