@@ -101,7 +101,7 @@ __device__ void block_sort_pairs(int n, uint32_t *key, uint32_t *val, uint32_t *
             const unsigned act = __ballot_sync(0xffffffffu, valid);
             if (valid) {
                 const unsigned d = (key[i] >> shift) & 255u;
-                const unsigned peers = __match_any_sync(act, d);
+                const unsigned peers = match_digit8(act, d);
                 if ((peers & lt) == 0) cnt[w][d] += __popc(peers);
             }
             __syncwarp();
@@ -149,7 +149,7 @@ __device__ void block_sort_pairs(int n, uint32_t *key, uint32_t *val, uint32_t *
                 k = key[i];
                 v = val[i];
                 d = (k >> shift) & 255u;
-                const unsigned peers = __match_any_sync(act, d);
+                const unsigned peers = match_digit8(act, d);
                 r = __popc(peers & lt);
                 cntp = __popc(peers);
                 prior = cnt[w][d];

@@ -25,7 +25,8 @@ void set_cuda_error(const char *what, cudaError_t e);
 
 // Barnes-Hut walk variants (all give identical forces): warp-synchronous;
 // one walk per thread at 6 blocks of 256 per SM (<= 40 registers); one walk
-// per thread with the registers the compiler wants.
+// per thread with the registers the compiler wants; one thread walking for
+// two or four Morton neighbours at once.
 enum {
     WALK_WARP = 0,
     WALK_THREAD = 1,
@@ -33,6 +34,29 @@ enum {
     WALK_PAIR = 3,
     WALK_QUAD = 4,
 };
+
+// Nanoseconds of the GPU's global timer (bounds of every device-side wait).
+__device__ __forceinline__ unsigned long long global_ns()
+{
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// The lanes of `act` whose 8-bit digit equals this lane's: eight ballots,
+// one per bit (the same mask as __match_any_sync, at ballot throughput).
+// Every lane of `act` must call it.
+__device__ __forceinline__ unsigned match_digit8(unsigned act, unsigned d)
+{
+    unsigned peers = act;
+#pragma unroll
+    for (int b = 0; b < 8; b++) {
+        const bool bit = (d >> b) & 1u;
+        const unsigned m = __ballot_sync(act, bit);
+        peers &= bit ? m : ~m;
+    }
+    return peers;
+}
 
 // Device-side status words (one int each in a session's `status` buffer).
 enum {

@@ -1195,12 +1195,6 @@ __device__ __forceinline__ uint32_t smem_addr(const void *p)
     return (uint32_t) __cvta_generic_to_shared(p);
 }
 
-__device__ __forceinline__ unsigned long long global_ns()
-{
-    unsigned long long t;
-    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-    return t;
-}
 
 __device__ __forceinline__ void mbar_init(uint64_t *bar, unsigned count)
 {

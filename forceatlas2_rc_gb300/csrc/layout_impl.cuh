@@ -138,7 +138,8 @@ template <class R> struct Layout : LayoutBase {
             ss.key_b = mem.get<uint32_t>(nn);
             ss.val_b = mem.get<uint32_t>(nn);
             ss.counts = mem.get<uint32_t>(sort_scratch_counts(n));
-            ss.digit_total = mem.get<uint32_t>(256);
+            ss.err = status + ST_ERROR;
+            ss.digit_total = mem.get<uint32_t>(SORT_AUX);
             psort = mem.get<R4>(nn);
             child = mem.get<int2>(nn - 1);
             range = mem.get<int2>(nn - 1);
@@ -246,6 +247,7 @@ template <class R> struct Layout : LayoutBase {
         for (auto &e : ev) FA2_TRY(cudaEventCreate(&e), "could not create a CUDA event", 1);
         mem.pool = opts ? opts->pool : nullptr;
         mem.s = s;
+        if (rep == FA2CU_REPULSION_BH && sort_setup()) return 1;
         if (rep == FA2CU_REPULSION_EXACT) {
             int sms = 0;
             cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
@@ -580,20 +582,30 @@ template <class R> struct Layout : LayoutBase {
         return 0;
     }
 
+    // The iteration graphs again, after an option changed the launches.
+    int recapture()
+    {
+        cudaSetDevice(device);
+        FA2_TRY(cudaStreamSynchronize(s), "the computation on the GPU failed", 1);
+        if (g1) cudaGraphExecDestroy(g1);
+        if (g8) cudaGraphExecDestroy(g8);
+        g1 = g8 = nullptr;
+        if (capture(&g1, 1)) return 1;
+        if (n <= (1 << 16) && capture(&g8, 8)) return 1;
+        return 0;
+    }
+
     int option(const char *name, double value) override
     {
+        if (!strcmp(name, "sort_threads") && (value == 256 || value == 512 || value == 1024)) {
+            ss.tile_threads = (int) value;
+            return recapture();
+        }
         if (!strcmp(name, "walk") &&
             (value == WALK_WARP || value == WALK_THREAD || value == WALK_THREAD_WIDE ||
              value == WALK_PAIR || value == WALK_QUAD)) {
             walk = (int) value;
-            cudaSetDevice(device);
-            FA2_TRY(cudaStreamSynchronize(s), "the computation on the GPU failed", 1);
-            if (g1) cudaGraphExecDestroy(g1);
-            if (g8) cudaGraphExecDestroy(g8);
-            g1 = g8 = nullptr;
-            if (capture(&g1, 1)) return 1;
-            if (n <= (1 << 16) && capture(&g8, 8)) return 1;
-            return 0;
+            return recapture();
         }
         set_message("unknown option %s = %g", name, value);
         return 1;

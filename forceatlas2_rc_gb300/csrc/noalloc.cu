@@ -37,8 +37,8 @@ constexpr size_t align256(size_t b) { return (b + 255) / 256 * 256; }
 constexpr size_t OFF_KEY_B = 0;
 constexpr size_t OFF_VAL_B = OFF_KEY_B + align256((size_t) NOALLOC_MAX_N * 4);
 constexpr size_t OFF_COUNTS = OFF_VAL_B + align256((size_t) NOALLOC_MAX_N * 4);
-constexpr size_t OFF_TOTAL = OFF_COUNTS + align256(256 * (size_t) NOALLOC_NB * 4);
-constexpr size_t OFF_PART = OFF_TOTAL + align256(256 * 4);
+constexpr size_t OFF_TOTAL = OFF_COUNTS + align256(4 * 256 * (size_t) NOALLOC_NB * 4);
+constexpr size_t OFF_PART = OFF_TOTAL + align256(SORT_AUX * 4);
 constexpr size_t OFF_BBOX = OFF_PART + align256(4 * (size_t) NOALLOC_NBBOX * 4);
 constexpr size_t OFF_QUANT = OFF_BBOX + align256(4 * 4);
 constexpr size_t OFF_TICKET = OFF_QUANT + align256(4 * 8);
@@ -95,6 +95,7 @@ extern "C" int fa2cu_morton_order_noalloc(int n, const float *pos, uint32_t *key
                                         ticket);
     k_morton<float><<<ceil_div(n, 256), 256, 0, s>>>(n, p2, (const double *) (base + OFF_QUANT),
                                                      key, order);
+    if (sort_setup()) return 1;
     SortScratch w;
     w.key_b = (uint32_t *) (base + OFF_KEY_B);
     w.val_b = (uint32_t *) (base + OFF_VAL_B);

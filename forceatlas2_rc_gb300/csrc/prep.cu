@@ -162,7 +162,7 @@ void prep_scratch(DevMem &mem, int n, int m, PrepScratch &ws)
     ws.sort.key_b = mem.get<uint32_t>(two_m);
     ws.sort.val_b = mem.get<uint32_t>(two_m);
     ws.sort.counts = mem.get<uint32_t>(sort_scratch_counts((int) two_m));
-    ws.sort.digit_total = mem.get<uint32_t>(256);
+    ws.sort.digit_total = mem.get<uint32_t>(SORT_AUX);
 }
 
 double prep_scratch_bytes(int n, int m)
@@ -205,6 +205,7 @@ long long prep_graph(cudaStream_t s, int n, int m, const int *from, const int *t
         int passes = 1;
         while (passes < 4 && ((uint64_t) n >> (8 * passes)) != 0) passes++;
         uint32_t *k = ws.key, *v = ws.val;
+        if (sort_setup()) return -1;
         sort_pairs_passes(s, 2 * m, k, v, ws.sort, passes, &k, &v);
         const double mean = (double) ((long long) n + 2LL * (long long) m) / (double) n;
         k_prep_fill<<<std::max(1, std::min(ceil_div(2 * m, 256), 152 * 16)), 256, 0, s>>>(

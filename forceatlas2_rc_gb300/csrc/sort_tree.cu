@@ -3,15 +3,18 @@
 //
 // Sort (reference pipeline.cl:132-188 / src/gpu_full.c:419-435, four passes
 // of 8 bits; any stable sort gives the reference's order, ties by index):
-//   hist    per block of SORT_TILE keys, its 256 digit counts (shared-memory
-//           counters fed by warp-aggregated increments: __match_any_sync
-//           groups the lanes with equal digits, one lane adds the group);
-//   scan    one block per digit: exclusive scan of that digit's counts over
-//           the blocks, and the digit's total;
-//   scatter each block ranks its keys stably with warp-ballot matching
-//           (lanes in order, rounds in order, warps in order), stages them
-//           by digit in shared memory, then writes runs of equal digits to
-//           consecutive global positions.
+//   hist4    one pass over the keys: the 256-bin histogram of every digit
+//            (shared-memory counters fed by warp-aggregated increments: the
+//            lanes with equal digits are found by eight ballots and one lane
+//            adds the group); the last block turns them into digit bases;
+//   onesweep one launch per digit: each block takes the next tile of 2048
+//            keys, ranks them stably (lanes, rounds and warps in order),
+//            publishes its per-digit counts, adds those of the tiles before
+//            it (decoupled look-back, bounded in time), stages the keys by
+//            digit in shared memory and writes runs of equal digits to
+//            consecutive global positions.
+#include <algorithm>
+
 #include "sort_tree.cuh"
 #include "karras.cuh"
 
@@ -22,31 +25,6 @@ __device__ __forceinline__ unsigned lanemask_lt()
     unsigned m;
     asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
     return m;
-}
-
-__global__ void __launch_bounds__(SORT_THREADS)
-k_sort_hist(int n, int shift, const uint32_t *__restrict__ key, uint32_t *__restrict__ counts,
-            int nb)
-{
-    __shared__ uint32_t h[256];
-    h[threadIdx.x] = 0;
-    __syncthreads();
-    const int base = blockIdx.x * SORT_TILE;
-    const int lane = threadIdx.x & 31;
-#pragma unroll 4
-    for (int it = 0; it < SORT_ITEMS; it++) {
-        const int idx = base + it * SORT_THREADS + threadIdx.x;
-        const bool valid = idx < n;
-        const unsigned act = __ballot_sync(0xffffffffu, valid);
-        if (valid) {
-            const unsigned d = (key[idx] >> shift) & 255u;
-            const unsigned peers = __match_any_sync(act, d);
-            if ((peers & lanemask_lt()) == 0) atomicAdd(&h[d], (uint32_t) __popc(peers));
-        }
-        (void) lane;
-    }
-    __syncthreads();
-    counts[threadIdx.x * nb + blockIdx.x] = h[threadIdx.x];
 }
 
 // Block-wide inclusive scan of one value per thread (blockDim.x <= 1024).
@@ -76,50 +54,111 @@ __device__ __forceinline__ uint32_t block_incl_scan(uint32_t v, uint32_t *warp_t
     return r;
 }
 
-__global__ void __launch_bounds__(1024)
-k_sort_scan(int nb, uint32_t *__restrict__ counts, uint32_t *__restrict__ digit_total)
+// Histograms of every digit of the keys (one pass), the status words of the
+// look-back zeroed; the last block to finish turns the histograms into digit
+// bases (exclusive scans).
+__global__ void __launch_bounds__(SORT_THREADS)
+k_sort_hist4(int n, int passes, const uint32_t *__restrict__ key, uint32_t *__restrict__ status,
+             size_t nstatus, uint32_t *__restrict__ aux)
 {
+    __shared__ uint32_t h[4][256];
     __shared__ uint32_t wt[32];
     __shared__ uint32_t tot;
-    uint32_t *c = counts + (size_t) blockIdx.x * nb;
-    uint32_t carry = 0;
-    for (int base = 0; base < nb; base += blockDim.x) {
-        const int i = base + threadIdx.x;
-        const uint32_t v = i < nb ? c[i] : 0;
-        const uint32_t incl = block_incl_scan(v, wt, &tot);
-        if (i < nb) c[i] = carry + incl - v;
-        carry += tot;
-        __syncthreads();
+    __shared__ int last;
+    for (int d = threadIdx.x; d < 4 * 256; d += SORT_THREADS) (&h[0][0])[d] = 0;
+    for (size_t i = (size_t) blockIdx.x * SORT_THREADS + threadIdx.x; i < nstatus;
+         i += (size_t) gridDim.x * SORT_THREADS)
+        status[i] = 0u;
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    (void) lane;
+    for (int idx0 = blockIdx.x * SORT_TILE; idx0 < n; idx0 += gridDim.x * SORT_TILE) {
+#pragma unroll 2
+        for (int it = 0; it < SORT_ITEMS; it++) {
+            const int idx = idx0 + it * SORT_THREADS + threadIdx.x;
+            const bool valid = idx < n;
+            const unsigned act = __ballot_sync(0xffffffffu, valid);
+            if (valid) {
+                const uint32_t k = key[idx];
+                for (int p = 0; p < passes; p++) {
+                    const unsigned d = (k >> (8 * p)) & 255u;
+                    const unsigned peers = match_digit8(act, d);
+                    if ((peers & lanemask_lt()) == 0) atomicAdd(&h[p][d], (uint32_t) __popc(peers));
+                }
+            }
+        }
     }
-    if (threadIdx.x == 0) digit_total[blockIdx.x] = carry;
+    __syncthreads();
+    for (int p = 0; p < passes; p++) {
+        const uint32_t c = h[p][threadIdx.x];
+        if (c) atomicAdd(aux + SORT_AUX_HIST + p * 256 + threadIdx.x, c);
+    }
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0)
+        last = atomicAdd(aux + SORT_AUX_DONE, 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    for (int p = 0; p < passes; p++) {
+        const uint32_t c = __ldcg(aux + SORT_AUX_HIST + p * 256 + threadIdx.x);
+        const uint32_t incl = block_incl_scan(c, wt, &tot);
+        aux[SORT_AUX_BASE + p * 256 + threadIdx.x] = incl - c;
+        aux[SORT_AUX_HIST + p * 256 + threadIdx.x] = 0u;
+    }
+    if (threadIdx.x < 4) aux[SORT_AUX_TICKET + threadIdx.x] = 0u;
+    if (threadIdx.x == 0) aux[SORT_AUX_DONE] = 0u;
 }
 
-__global__ void __launch_bounds__(SORT_THREADS)
-k_sort_scatter(int n, int shift, const uint32_t *__restrict__ kin, const uint32_t *__restrict__ vin,
-               const uint32_t *__restrict__ counts, const uint32_t *__restrict__ digit_total,
-               uint32_t *__restrict__ kout, uint32_t *__restrict__ vout, int nb)
+// Look-back words: the tile's count of a digit, or (once known) the count of
+// every tile up to and including it.
+constexpr uint32_t LB_COUNT = 1u << 30, LB_PREFIX = 1u << 31, LB_MASK = LB_COUNT - 1u;
+
+__device__ __forceinline__ void lb_store(uint32_t *p, uint32_t v)
 {
-    constexpr int NW = SORT_THREADS / 32;
-    constexpr int PER_WARP = SORT_TILE / NW; // contiguous keys per warp
+    asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ uint32_t lb_load(const uint32_t *p)
+{
+    uint32_t v;
+    asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// One pass: each block takes the next tile of T * SORT_ITEMS keys (tickets
+// in launch order, so a block only ever waits for tiles of blocks that
+// started before it), ranks its keys stably (warp-contiguous chunks, lanes
+// and rounds in order, warp matching), publishes its digit counts, adds its
+// predecessors' (look-back in windows of 16 tiles, bounded in time) and
+// scatters through shared memory in runs of equal digits. Dynamic shared
+// memory: per-warp digit counters, then the staged keys and values.
+template <int T>
+__global__ void __launch_bounds__(T)
+k_sort_onesweep(int n, int pass, const uint32_t *__restrict__ kin,
+                const uint32_t *__restrict__ vin, uint32_t *__restrict__ kout,
+                uint32_t *__restrict__ vout, uint32_t *__restrict__ status,
+                uint32_t *__restrict__ aux, int *__restrict__ err)
+{
+    constexpr int NW = T / 32;
+    constexpr int TILE = T * SORT_ITEMS;
+    constexpr int PER_WARP = TILE / NW; // contiguous keys per warp
     constexpr int ROUNDS = PER_WARP / 32;
-    __shared__ uint32_t wh[NW][256];
+    extern __shared__ __align__(16) uint32_t dsm[];
+    uint32_t(*wh)[256] = reinterpret_cast<uint32_t(*)[256]>(dsm);
+    uint32_t *sk = dsm + NW * 256, *sv = sk + TILE;
     __shared__ uint32_t lbase[256], gbase[256];
     __shared__ uint32_t wt[32];
     __shared__ uint32_t tot;
-    __shared__ uint32_t sk[SORT_TILE], sv[SORT_TILE];
+    __shared__ int tile_s;
 
+    const int shift = 8 * pass;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    for (int d = threadIdx.x; d < NW * 256; d += SORT_THREADS) (&wh[0][0])[d] = 0;
-    // global start of each digit: exclusive scan of the digit totals, plus
-    // this block's offset inside the digit
-    {
-        const uint32_t t = digit_total[threadIdx.x];
-        const uint32_t incl = block_incl_scan(t, wt, &tot);
-        gbase[threadIdx.x] = incl - t + counts[threadIdx.x * nb + blockIdx.x];
-    }
+    if (threadIdx.x == 0) tile_s = (int) atomicAdd(aux + SORT_AUX_TICKET + pass, 1u);
+    for (int d = threadIdx.x; d < NW * 256; d += T) dsm[d] = 0;
     __syncthreads();
+    const int tile = tile_s;
 
-    const int base = blockIdx.x * SORT_TILE + w * PER_WARP;
+    const int base = tile * TILE + w * PER_WARP;
     uint32_t k[ROUNDS], v[ROUNDS];
     uint32_t rk[ROUNDS];
 #pragma unroll
@@ -132,7 +171,7 @@ k_sort_scatter(int n, int shift, const uint32_t *__restrict__ kin, const uint32_
         uint32_t prior = 0, lt = 0, cnt = 0;
         unsigned d = (k[r] >> shift) & 255u;
         if (valid) {
-            const unsigned peers = __match_any_sync(act, d);
+            const unsigned peers = match_digit8(act, d);
             lt = __popc(peers & lanemask_lt());
             cnt = __popc(peers);
             prior = wh[w][d];
@@ -143,34 +182,75 @@ k_sort_scatter(int n, int shift, const uint32_t *__restrict__ kin, const uint32_
         rk[r] = valid ? prior + lt : 0xffffffffu;
     }
     __syncthreads();
-    // per digit: exclusive prefix over the warps, and the block's count
-    {
+    // per digit (threads 0..255): exclusive prefix over the warps, the
+    // tile's count, then the tile's offset inside the digit from the
+    // look-back
+    uint32_t run = 0;
+    if (threadIdx.x < 256) {
         const int d = threadIdx.x;
-        uint32_t run = 0;
-#pragma unroll
+#pragma unroll 8
         for (int ww = 0; ww < NW; ww++) {
             const uint32_t c = wh[ww][d];
             wh[ww][d] = run;
             run += c;
         }
-        const uint32_t incl = block_incl_scan(run, wt, &tot);
-        lbase[d] = incl - run;
+        uint32_t *me = status + (size_t) tile * 256 + d;
+        uint32_t excl = 0;
+        if (tile == 0) {
+            lb_store(me, LB_PREFIX | run);
+        } else {
+            lb_store(me, LB_COUNT | run);
+            const unsigned long long t0 = global_ns();
+            bool gave_up = false;
+            // windows of 16 predecessors, loaded together, used in order
+            // until a prefix (done) or a word not yet published (load again)
+            for (int j = tile - 1; j >= 0;) {
+                uint32_t x[16];
+#pragma unroll
+                for (int q = 0; q < 16; q++)
+                    x[q] = j - q >= 0 ? lb_load(status + (size_t) (j - q) * 256 + d) : LB_PREFIX;
+                bool done = false, stalled = false;
+#pragma unroll
+                for (int q = 0; q < 16; q++) {
+                    if (done || stalled) continue;
+                    if (x[q] & LB_PREFIX) {
+                        excl += x[q] & LB_MASK;
+                        done = true;
+                    } else if (x[q] & LB_COUNT) {
+                        excl += x[q] & LB_MASK;
+                        j--;
+                    } else {
+                        stalled = true;
+                    }
+                }
+                if (done) break;
+                if (stalled && global_ns() - t0 > 1000000000ull) {
+                    gave_up = true; // 1 s: a predecessor never published
+                    break;
+                }
+            }
+            if (gave_up && err) atomicOr(err, ERR_WAIT);
+            lb_store(me, LB_PREFIX | ((excl + run) & LB_MASK));
+        }
+        gbase[d] = aux[SORT_AUX_BASE + pass * 256 + d] + excl;
     }
+    const uint32_t incl = block_incl_scan(run, wt, &tot); // threads >= 256 add 0
+    if (threadIdx.x < 256) lbase[threadIdx.x] = incl - run;
     __syncthreads();
 #pragma unroll
     for (int r = 0; r < ROUNDS; r++) {
         if (rk[r] == 0xffffffffu) continue;
         const unsigned d = (k[r] >> shift) & 255u;
         const uint32_t p = lbase[d] + wh[w][d] + rk[r];
-        if (p < (uint32_t) SORT_TILE) { // always, for consistent counts
+        if (p < (uint32_t) TILE) { // always, for consistent counts
             sk[p] = k[r];
             sv[p] = v[r];
         }
     }
     __syncthreads();
-    const int tile0 = blockIdx.x * SORT_TILE;
-    const int cnt_tile = min(SORT_TILE, n - tile0);
-    for (int i = threadIdx.x; i < cnt_tile; i += SORT_THREADS) {
+    const int tile0 = tile * TILE;
+    const int cnt_tile = min(TILE, n - tile0);
+    for (int i = threadIdx.x; i < cnt_tile; i += T) {
         const uint32_t key = sk[i];
         const unsigned d = (key >> shift) & 255u;
         const uint32_t g = gbase[d] + (uint32_t) i - lbase[d];
@@ -181,19 +261,54 @@ k_sort_scatter(int n, int shift, const uint32_t *__restrict__ kin, const uint32_
     }
 }
 
-size_t sort_scratch_counts(int n) { return 256 * (size_t) ceil_div(n, SORT_TILE); }
+template <int T> constexpr size_t onesweep_smem()
+{
+    return ((size_t) (T / 32) * 256 + 2 * (size_t) T * SORT_ITEMS) * sizeof(uint32_t);
+}
+
+int sort_setup()
+{
+    // the opt-in above 48 KB of dynamic shared memory of the larger tiles
+    FA2_TRY(cudaFuncSetAttribute(k_sort_onesweep<512>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int) onesweep_smem<512>()),
+            "cudaFuncSetAttribute", 1);
+    FA2_TRY(cudaFuncSetAttribute(k_sort_onesweep<1024>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int) onesweep_smem<1024>()),
+            "cudaFuncSetAttribute", 1);
+    return 0;
+}
+
+template <int T>
+static void onesweep_pass(cudaStream_t s, int n, int pass, const uint32_t *kin,
+                          const uint32_t *vin, uint32_t *kout, uint32_t *vout,
+                          const SortScratch &w)
+{
+    const int nb = ceil_div(n, T * SORT_ITEMS);
+    k_sort_onesweep<T><<<nb, T, onesweep_smem<T>(), s>>>(
+        n, pass, kin, vin, kout, vout, w.counts + (size_t) pass * 256 * nb, w.digit_total, w.err);
+}
+
+size_t sort_scratch_counts(int n) { return 4 * 256 * (size_t) ceil_div(n, SORT_TILE); }
 
 void sort_pairs_passes(cudaStream_t s, int n, uint32_t *key, uint32_t *val,
                        const SortScratch &w, int passes, uint32_t **kout, uint32_t **vout)
 {
     const int nb = ceil_div(n, SORT_TILE);
+    const int hist_blocks = std::min(nb, 152 * 4);
+    // histograms, bases and tickets start at zero
+    cudaMemsetAsync(w.digit_total, 0, SORT_AUX * sizeof(uint32_t), s);
+    k_sort_hist4<<<hist_blocks, SORT_THREADS, 0, s>>>(n, passes, key, w.counts,
+                                                     (size_t) passes * 256 * nb, w.digit_total);
     uint32_t *ka = key, *va = val, *kb = w.key_b, *vb = w.val_b;
     for (int pass = 0; pass < passes; pass++) {
-        const int shift = 8 * pass;
-        k_sort_hist<<<nb, SORT_THREADS, 0, s>>>(n, shift, ka, w.counts, nb);
-        k_sort_scan<<<256, 1024, 0, s>>>(nb, w.counts, w.digit_total);
-        k_sort_scatter<<<nb, SORT_THREADS, 0, s>>>(n, shift, ka, va, w.counts, w.digit_total,
-                                                   kb, vb, nb);
+        if (w.tile_threads == 1024)
+            onesweep_pass<1024>(s, n, pass, ka, va, kb, vb, w);
+        else if (w.tile_threads == 512)
+            onesweep_pass<512>(s, n, pass, ka, va, kb, vb, w);
+        else
+            onesweep_pass<256>(s, n, pass, ka, va, kb, vb, w);
         uint32_t *t = ka;
         ka = kb;
         kb = t;
