@@ -174,6 +174,11 @@ k_bbox(int n, const typename RT<R>::R2 *__restrict__ pos, R *__restrict__ partia
         quant[0] = (double) a;
         quant[1] = (double) b;
         quant[2] = extent > 0.0 ? __ddiv_rn(65535.0, extent) : 0.0;
+        // the scale as a float-float pair (hi, lo) in the last slot, for
+        // the float quantisation of k_morton
+        float *qf = reinterpret_cast<float *>(quant + 3);
+        qf[0] = (float) quant[2];
+        qf[1] = (float) (quant[2] - (double) qf[0]);
         *ticket = 0u;
     }
 }
@@ -194,6 +199,45 @@ __device__ __forceinline__ uint32_t spread16(uint32_t v)
 // widen exactly), so that a layout's tree depends on its positions only, not
 // on the precision of the iteration: the FP32 path builds the tree of the
 // reference's double construction.
+// Quantised coordinate of the Morton code: trunc(clamp((v - min) scale,
+// 0, 65535)) with the subtraction and the product rounded in double
+// (pipeline.cl:105-130).
+__device__ __forceinline__ uint32_t morton_cell(double v, double mn, double scale)
+{
+    const double f = cl_min(cl_max(__dmul_rn(__dsub_rn(v, mn), scale), 0.0), 65535.0);
+    return (uint32_t) f;
+}
+// The same for a float coordinate, from float arithmetic: the difference
+// exactly (TwoSum) and the product with the scale's float-float pair (sh,
+// sl) to about 2^-46 relative, i.e. within 1e-9 of the real value, as the
+// double computation is within 2e-11. Away from an integer (by 1e-7) and
+// from the clamps both truncate alike; the rare others are computed in
+// double. (FP64 throughput on this GPU is a small fraction of FP32's.)
+__device__ __forceinline__ uint32_t morton_cell(float v, double mn, double scale, float sh,
+                                                float sl)
+{
+    const float m = (float) mn;                    // exact: mn is a float
+    const float d = v - m;                         // TwoSum of v and -m
+    const float bv = d - v;
+    const float e = (v - (d - bv)) + (-m - bv);    // v - m = d + e exactly
+    const float p = d * sh;
+    const float pe = fmaf(d, sh, -p);              // d sh = p + pe exactly
+    const float lo = fmaf(d, sl, fmaf(e, sh, pe)); // the rest, to 2^-46
+    float t = truncf(p);
+    float fr = (p - t) + lo;                       // p - t exact below 2^24
+    if (fr < 0.0f) {
+        t -= 1.0f;
+        fr += 1.0f;
+    } else if (fr >= 1.0f) {
+        t += 1.0f;
+        fr -= 1.0f;
+    }
+    // (a scale below 1e-30 may have a flushed low part: double path)
+    if (p > 1.0f && p < 65534.0f && fr > 1e-7f && fr < 1.0f - 1e-7f && sh > 1e-30f)
+        return (uint32_t) t;
+    return morton_cell((double) v, mn, scale);
+}
+
 template <class R>
 __global__ void __launch_bounds__(256)
 k_morton(int n, const typename RT<R>::R2 *__restrict__ pos, const double *__restrict__ quant,
@@ -203,11 +247,17 @@ k_morton(int n, const typename RT<R>::R2 *__restrict__ pos, const double *__rest
     if (i >= n) return;
     const double minx = quant[0], miny = quant[1], scale = quant[2];
     const typename RT<R>::R2 p = pos[i];
-    const double fx =
-        cl_min(cl_max(__dmul_rn(__dsub_rn((double) p.x, minx), scale), 0.0), 65535.0);
-    const double fy =
-        cl_min(cl_max(__dmul_rn(__dsub_rn((double) p.y, miny), scale), 0.0), 65535.0);
-    key[i] = spread16((uint32_t) fx) | (spread16((uint32_t) fy) << 1);
+    uint32_t cx, cy;
+    if constexpr (sizeof(R) == 4) {
+        const float *qf = reinterpret_cast<const float *>(quant + 3);
+        const float sh = qf[0], sl = qf[1];
+        cx = morton_cell(p.x, minx, scale, sh, sl);
+        cy = morton_cell(p.y, miny, scale, sh, sl);
+    } else {
+        cx = morton_cell(p.x, minx, scale);
+        cy = morton_cell(p.y, miny, scale);
+    }
+    key[i] = spread16(cx) | (spread16(cy) << 1);
     idx[i] = (uint32_t) i;
 }
 

@@ -110,6 +110,73 @@ def test_tree_bit_exact_oracle(gpu, orc, prec, n, dup):
         assert_ni_single(t["ni"], r["ni"])
 
 
+@pytest.mark.parametrize("span", [2e3, 7.3, 3e6])
+def test_morton_keys_at_cell_boundaries(gpu, orc, span):
+    """FP32 Morton keys (float-float quantisation, double fallback near a
+    cell boundary) equal the double construction's for float positions placed
+    within a few ulps of the quantisation boundaries (v - min) * scale = k,
+    at three extents."""
+    rng = np.random.default_rng(int(span))
+    n = 60000
+    lo = -0.37 * span
+    scale = 65535.0 / span
+    k = rng.integers(0, 65536, size=(n, 2)).astype(np.float64)
+    pos = lo + k / scale
+    pos = np.nextafter(pos.astype(np.float32),
+                       np.where(rng.random((n, 2)) < 0.5, -np.inf, np.inf).astype(np.float32))
+    pos = pos.astype(np.float64)
+    pos[:3] = [[lo, lo], [lo + span, lo + span], [lo + span / 2, lo]]  # the extent
+    pos = f32(pos)
+    m = np.ones(n)
+    a = np.zeros(0, np.int32)
+    g = Graph(n, a, a, np.zeros(0))
+    g.mass = m
+    with Layout(g, pos, precision="single") as L:
+        t = L.tree(pos)
+    r = orc.pipe_build(n, pos, m, "d")
+    np.testing.assert_array_equal(t["key"], r["key"])
+    np.testing.assert_array_equal(t["order"], r["order"])
+
+
+def morton_np(pos):
+    """Morton keys of the double construction (pipeline.cl:105-130) in numpy:
+    IEEE double subtraction and product, clamp, truncate, interleave."""
+    mn = pos.min(axis=0)
+    ext = max(pos[:, 0].max() - mn[0], pos[:, 1].max() - mn[1])
+    scale = 65535.0 / ext if ext > 0 else 0.0
+    q = np.clip((pos - mn) * scale, 0.0, 65535.0).astype(np.uint32)
+
+    def spread(v):
+        v = v.astype(np.uint64)
+        v = (v | (v << 8)) & 0x00FF00FF
+        v = (v | (v << 4)) & 0x0F0F0F0F
+        v = (v | (v << 2)) & 0x33333333
+        v = (v | (v << 1)) & 0x55555555
+        return v
+    return (spread(q[:, 0]) | (spread(q[:, 1]) << 1)).astype(np.uint32)
+
+
+@pytest.mark.parametrize("prec", ["single", "double"])
+def test_sort_large_with_ties(gpu, prec):
+    """3,000,000 nodes, a third of them on 1000 shared positions: the device
+    keys and order equal numpy's keys and stable argsort (ties by index)."""
+    rng = np.random.default_rng(17)
+    n = 3_000_000
+    pos = rng.uniform(-5e3, 5e3, size=(n, 2))
+    dup = rng.random(n) < 0.33
+    pos[dup] = pos[rng.integers(0, 1000, dup.sum())]
+    if prec == "single":
+        pos = f32(pos)
+    a = np.zeros(0, np.int32)
+    g = Graph(n, a, a, np.zeros(0))
+    with Layout(g, pos, precision=prec) as L:
+        t = L.tree(pos)
+    key = morton_np(pos)
+    order = np.argsort(key, kind="stable")
+    np.testing.assert_array_equal(t["order"], order)
+    np.testing.assert_array_equal(t["key"], key[order])
+
+
 PIPE_SETS = [dict(), dict(linlog=True, adjust=True, theta=0.5),
              dict(strong=True, theta=0.0), dict(outbound=True, gravity=0.0)]
 
