@@ -174,11 +174,14 @@ k_bbox(int n, const typename RT<R>::R2 *__restrict__ pos, R *__restrict__ partia
         quant[0] = (double) a;
         quant[1] = (double) b;
         quant[2] = extent > 0.0 ? __ddiv_rn(65535.0, extent) : 0.0;
-        // the scale as a float-float pair (hi, lo) in the last slot, for
-        // the float quantisation of k_morton
-        float *qf = reinterpret_cast<float *>(quant + 3);
+        // for the float quantisation of k_morton: the scale as a float-float
+        // pair (hi, lo) and the minima as floats, 16-byte aligned in slots
+        // 4 and 5
+        float *qf = reinterpret_cast<float *>(quant + 4);
         qf[0] = (float) quant[2];
         qf[1] = (float) (quant[2] - (double) qf[0]);
+        qf[2] = a;
+        qf[3] = b;
         *ticket = 0u;
     }
 }
@@ -213,10 +216,9 @@ __device__ __forceinline__ uint32_t morton_cell(double v, double mn, double scal
 // double computation is within 2e-11. Away from an integer (by 1e-7) and
 // from the clamps both truncate alike; the rare others are computed in
 // double. (FP64 throughput on this GPU is a small fraction of FP32's.)
-__device__ __forceinline__ uint32_t morton_cell(float v, double mn, double scale, float sh,
-                                                float sl)
+__device__ __forceinline__ uint32_t morton_cell(float v, float m, double mn, double scale,
+                                                float sh, float sl)
 {
-    const float m = (float) mn;                    // exact: mn is a float
     const float d = v - m;                         // TwoSum of v and -m
     const float bv = d - v;
     const float e = (v - (d - bv)) + (-m - bv);    // v - m = d + e exactly
@@ -249,10 +251,9 @@ k_morton(int n, const typename RT<R>::R2 *__restrict__ pos, const double *__rest
     const typename RT<R>::R2 p = pos[i];
     uint32_t cx, cy;
     if constexpr (sizeof(R) == 4) {
-        const float *qf = reinterpret_cast<const float *>(quant + 3);
-        const float sh = qf[0], sl = qf[1];
-        cx = morton_cell(p.x, minx, scale, sh, sl);
-        cy = morton_cell(p.y, miny, scale, sh, sl);
+        const float4 qf = *reinterpret_cast<const float4 *>(quant + 4);
+        cx = morton_cell(p.x, qf.z, minx, scale, qf.x, qf.y);
+        cy = morton_cell(p.y, qf.w, miny, scale, qf.x, qf.y);
     } else {
         cx = morton_cell(p.x, minx, scale);
         cy = morton_cell(p.y, miny, scale);

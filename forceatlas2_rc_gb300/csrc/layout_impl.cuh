@@ -76,7 +76,7 @@ template <class R> struct Layout : LayoutBase {
     int *inc_off = nullptr;
     Inc<R> *inc = nullptr;
     R *bbox = nullptr, *bbox_partial = nullptr;
-    double *quant = nullptr; // min x, min y, Morton scale
+    double *quant = nullptr; // min x, min y, Morton scale, -, 4 floats (k_bbox)
     int nbbox = 1, nswing = 1;
     uint32_t *key = nullptr, *order = nullptr;
     SortScratch ss{};
@@ -131,7 +131,7 @@ template <class R> struct Layout : LayoutBase {
         if (want_tree) {
             nbbox = std::min(ceil_div(n, 256), 152 * 4);
             bbox = mem.get<R>(4);
-            quant = mem.get<double>(4);
+            quant = mem.get<double>(6);
             bbox_partial = mem.get<R>(4 * (size_t) nbbox);
             key = mem.get<uint32_t>(nn);
             order = mem.get<uint32_t>(nn);

@@ -41,7 +41,7 @@ constexpr size_t OFF_TOTAL = OFF_COUNTS + align256(4 * 256 * (size_t) NOALLOC_NB
 constexpr size_t OFF_PART = OFF_TOTAL + align256(SORT_AUX * 4);
 constexpr size_t OFF_BBOX = OFF_PART + align256(4 * (size_t) NOALLOC_NBBOX * 4);
 constexpr size_t OFF_QUANT = OFF_BBOX + align256(4 * 4);
-constexpr size_t OFF_TICKET = OFF_QUANT + align256(4 * 8);
+constexpr size_t OFF_TICKET = OFF_QUANT + align256(6 * 8);
 constexpr size_t NOALLOC_BYTES = OFF_TICKET + align256(4);
 
 // The scratch memory of fa2cu_morton_order_noalloc (one copy per device).
