@@ -53,6 +53,9 @@ WALKS = {"warp": 0, "thread": 1, "wide": 2, "pair": 3, "quad": 4}
 # algorithmic HBM bytes per node of the traversal: psort record 16, order 4,
 # force write 8 (FP32)
 TRAVERSE_HBM_BYTES_PER_NODE = 28
+# DRAM bytes (read + write) of one traversal launch on this workload, from
+# one ncu capture (profiles/kernels_sbm1m_full.md)
+TRAVERSE_DRAM_BYTES = 48.21e6 + 0.73e6
 
 
 def make_workload(small: bool = False):
@@ -737,7 +740,9 @@ def main():
     l2_bytes = 32.0 * counts["visits"] + 16.0 * counts["pairs"]
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"],
                 "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"],
-                "traffic": None,
+                "traffic": TRAVERSE_DRAM_BYTES if n == 1_000_000 else None,
+                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, "
+                                  "one launch (profiles/kernels_sbm1m_full.md)",
                 "kernel": {"warp": "k_traverse_warp<float>",
                            "thread": "k_traverse<float, 6>",
                            "wide": "k_traverse<float, 1>",

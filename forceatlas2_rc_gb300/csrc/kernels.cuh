@@ -1015,7 +1015,13 @@ k_swing(int n, const typename RT<R>::R2 *__restrict__ f,
             at = __dadd_rn(at, (double) t);
         }
     }
-    // per warp and per block, in a fixed tree order
+    // per warp and per block, in a fixed tree order: float-float in the FP32
+    // path (one conversion to double per block), double with compensation
+    // in the FP64 path
+    __shared__ double ss[8], st_[8];
+    __shared__ ff2 fss[8], fst[8];
+    __shared__ int last;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     if constexpr (sizeof(R) == 4) {
         for (int o = 16; o > 0; o >>= 1) {
             fs = ff_add(fs, ff2{__shfl_down_sync(0xffffffffu, fs.hi, o),
@@ -1023,27 +1029,35 @@ k_swing(int n, const typename RT<R>::R2 *__restrict__ f,
             ft = ff_add(ft, ff2{__shfl_down_sync(0xffffffffu, ft.hi, o),
                                 __shfl_down_sync(0xffffffffu, ft.lo, o)});
         }
-        as = ff_to_double(fs);
-        at = ff_to_double(ft);
+        if (lane == 0) {
+            fss[w] = fs;
+            fst[w] = ft;
+        }
     } else {
         as = warp_sum(as);
         at = warp_sum(at);
-    }
-    __shared__ double ss[8], st_[8];
-    __shared__ int last;
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    if (lane == 0) {
-        ss[w] = as;
-        st_[w] = at;
+        if (lane == 0) {
+            ss[w] = as;
+            st_[w] = at;
+        }
     }
     __syncthreads();
     if (threadIdx.x == 0) {
-        double a = 0.0, b = 0.0, ca = 0.0, cb = 0.0;
-        for (int k = 0; k < (int) (blockDim.x >> 5); k++) {
-            neumaier(a, ca, ss[k]);
-            neumaier(b, cb, st_[k]);
+        if constexpr (sizeof(R) == 4) {
+            ff2 a = fss[0], b = fst[0];
+            for (int k = 1; k < (int) (blockDim.x >> 5); k++) {
+                a = ff_add(a, fss[k]);
+                b = ff_add(b, fst[k]);
+            }
+            partial[blockIdx.x] = make_double2(ff_to_double(a), ff_to_double(b));
+        } else {
+            double a = 0.0, b = 0.0, ca = 0.0, cb = 0.0;
+            for (int k = 0; k < (int) (blockDim.x >> 5); k++) {
+                neumaier(a, ca, ss[k]);
+                neumaier(b, cb, st_[k]);
+            }
+            partial[blockIdx.x] = make_double2(__dadd_rn(a, ca), __dadd_rn(b, cb));
         }
-        partial[blockIdx.x] = make_double2(__dadd_rn(a, ca), __dadd_rn(b, cb));
         __threadfence();
         last = atomicAdd(ticket, 1u) == gridDim.x - 1;
     }

@@ -122,7 +122,7 @@ template <class R> struct Layout : LayoutBase {
         fixed = any_fixed ? mem.get<uint8_t>(nn) : nullptr;
         inc_off = mem.get<int>(nn + 1);
         inc = mem.get<Inc<R>>((size_t) ninc);
-        nswing = std::min(ceil_div(n, 256), 152 * 8);
+        nswing = std::min(ceil_div(n, 256), 152 * 2);
         swing_partial = mem.get<double2>((size_t) nswing);
         st = mem.get<SpeedState>(1);
         status = mem.get<int>(ST_COUNT);

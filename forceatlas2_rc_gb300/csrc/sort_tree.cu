@@ -4,9 +4,9 @@
 // Sort (reference pipeline.cl:132-188 / src/gpu_full.c:419-435, four passes
 // of 8 bits; any stable sort gives the reference's order, ties by index):
 //   hist4    one pass over the keys: the 256-bin histogram of every digit
-//            (shared-memory counters fed by warp-aggregated increments: the
-//            lanes with equal digits are found by eight ballots and one lane
-//            adds the group); the last block turns them into digit bases;
+//            (per-warp shared-memory counters, summed over the warps and
+//            added to the global counts); the last block turns them into
+//            digit bases;
 //   onesweep one launch per digit: each block takes the next tile of 2048
 //            keys, ranks them stably (lanes, rounds and warps in order),
 //            publishes its per-digit counts, adds those of the tiles before
@@ -61,36 +61,28 @@ __global__ void __launch_bounds__(SORT_THREADS)
 k_sort_hist4(int n, int passes, const uint32_t *__restrict__ key, uint32_t *__restrict__ status,
              size_t nstatus, uint32_t *__restrict__ aux)
 {
-    __shared__ uint32_t h[4][256];
+    // per-warp counters (shared-memory atomics, contention within a warp
+    // only), summed over the warps at the end
+    constexpr int NW = SORT_THREADS / 32;
+    __shared__ uint32_t h[NW][4][256];
     __shared__ uint32_t wt[32];
     __shared__ uint32_t tot;
     __shared__ int last;
-    for (int d = threadIdx.x; d < 4 * 256; d += SORT_THREADS) (&h[0][0])[d] = 0;
+    for (int d = threadIdx.x; d < NW * 4 * 256; d += SORT_THREADS) (&h[0][0][0])[d] = 0;
     for (size_t i = (size_t) blockIdx.x * SORT_THREADS + threadIdx.x; i < nstatus;
          i += (size_t) gridDim.x * SORT_THREADS)
         status[i] = 0u;
     __syncthreads();
-    const int lane = threadIdx.x & 31;
-    (void) lane;
-    for (int idx0 = blockIdx.x * SORT_TILE; idx0 < n; idx0 += gridDim.x * SORT_TILE) {
-#pragma unroll 2
-        for (int it = 0; it < SORT_ITEMS; it++) {
-            const int idx = idx0 + it * SORT_THREADS + threadIdx.x;
-            const bool valid = idx < n;
-            const unsigned act = __ballot_sync(0xffffffffu, valid);
-            if (valid) {
-                const uint32_t k = key[idx];
-                for (int p = 0; p < passes; p++) {
-                    const unsigned d = (k >> (8 * p)) & 255u;
-                    const unsigned peers = match_digit8(act, d);
-                    if ((peers & lanemask_lt()) == 0) atomicAdd(&h[p][d], (uint32_t) __popc(peers));
-                }
-            }
-        }
+    const int w = threadIdx.x >> 5;
+    for (int idx = blockIdx.x * SORT_THREADS + threadIdx.x; idx < n;
+         idx += gridDim.x * SORT_THREADS) {
+        const uint32_t k = key[idx];
+        for (int p = 0; p < passes; p++) atomicAdd(&h[w][p][(k >> (8 * p)) & 255u], 1u);
     }
     __syncthreads();
     for (int p = 0; p < passes; p++) {
-        const uint32_t c = h[p][threadIdx.x];
+        uint32_t c = 0;
+        for (int ww = 0; ww < NW; ww++) c += h[ww][p][threadIdx.x];
         if (c) atomicAdd(aux + SORT_AUX_HIST + p * 256 + threadIdx.x, c);
     }
     __threadfence();
