@@ -69,7 +69,7 @@ FULL_TIME_NAMES = ("total", "codes", "sort", "tree", "repulsion",
 class ServerConfig(C.Structure):
     """fa2cu_server_config (include/fa2_cuda.h)."""
     _fields_ = [("device", C.c_int), ("hbm_budget", C.c_double),
-                ("max_jobs", C.c_int), ("chunk", C.c_int)]
+                ("max_jobs", C.c_int), ("chunk", C.c_int), ("policy", C.c_int)]
 
 
 def dptr(a):

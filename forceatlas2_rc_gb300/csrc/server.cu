@@ -3,7 +3,8 @@
 //
 // Three kinds of host thread meet here:
 //   - callers: submit (the job's arrays are copied) and wait / collect;
-//   - the admission thread: takes queued jobs in arrival order while fewer
+//   - the admission thread: takes queued jobs (in arrival order, or least
+//     work first) while fewer
 //     than max_jobs are resident and their estimated device footprint fits
 //     the budget, and opens each one (graph upload, buffers from the
 //     server's memory pool, CUDA graphs of its iteration) on a stream of its
@@ -77,7 +78,7 @@ struct Job {
 };
 
 struct Server {
-    int device = 0, max_jobs = 16, chunk = 16;
+    int device = 0, max_jobs = 16, chunk = 16, policy = FA2CU_ADMIT_ARRIVAL;
     static constexpr int DEPTH = 2; // chunks in flight per job
     double budget = 0.0;
     cudaMemPool_t pool = nullptr;
@@ -97,6 +98,7 @@ struct Server {
     std::thread admit_th, sched_th;
 
     void admit_loop();
+    std::deque<Job *>::iterator next_job();
     void sched_loop();
     void finish(Job *j);
     int priority_of(const fa2_full_params &p) const;
@@ -112,6 +114,22 @@ int Server::priority_of(const fa2_full_params &p) const
     return prio_greatest + (int) std::lround(t * (double) (prio_least - prio_greatest));
 }
 
+// The queued job to admit next: the first one, or the one of least work.
+std::deque<Job *>::iterator Server::next_job()
+{
+    if (policy != FA2CU_ADMIT_LEAST_WORK) return queue.begin();
+    auto best = queue.begin();
+    double bw = 0.0;
+    for (auto it = queue.begin(); it != queue.end(); ++it) {
+        const double wk = (double) (*it)->p.n * (double) std::max((*it)->p.iterations, 1);
+        if (it == queue.begin() || wk < bw) {
+            best = it;
+            bw = wk;
+        }
+    }
+    return best;
+}
+
 void Server::admit_loop()
 {
     cudaSetDevice(device);
@@ -122,11 +140,12 @@ void Server::admit_loop()
             cv_admit.wait(lk, [&] {
                 if (stop) return true;
                 if (queue.empty() || resident >= max_jobs) return false;
-                return used + queue.front()->footprint <= budget;
+                return used + (*next_job())->footprint <= budget;
             });
             if (stop) return;
-            j = queue.front();
-            queue.pop_front();
+            auto it = next_job();
+            j = *it;
+            queue.erase(it);
             resident++;
             used += j->footprint;
             peak_used = std::max(peak_used, used);
@@ -306,6 +325,8 @@ fa2cu_server *fa2cu_server_open(const fa2cu_server_config *cfg)
     S->device = cfg->device;
     S->max_jobs = cfg->max_jobs > 0 ? cfg->max_jobs : 16;
     S->chunk = cfg->chunk > 0 ? cfg->chunk : 16;
+    S->policy = cfg->policy == FA2CU_ADMIT_LEAST_WORK ? FA2CU_ADMIT_LEAST_WORK
+                                                     : FA2CU_ADMIT_ARRIVAL;
     size_t fr = 0, tot = 0;
     cudaMemGetInfo(&fr, &tot);
     S->budget = cfg->hbm_budget > 0 ? cfg->hbm_budget : 0.8 * (double) fr;

@@ -33,14 +33,19 @@ class Server:
 
     ``hbm_budget`` (bytes; None: 80 % of the free memory) bounds the summed
     footprint of the resident jobs, ``max_jobs`` their number; ``chunk`` is
-    the number of iterations enqueued per job at a time.
+    the number of iterations enqueued per job at a time; ``policy`` the
+    admission order, "arrival" or "least_work" (nodes x iterations).
     """
 
+    POLICIES = {"arrival": 0, "least_work": 1}
+
     def __init__(self, device: int = 0, hbm_budget: float | None = None,
-                 max_jobs: int = 16, chunk: int = 16):
+                 max_jobs: int = 16, chunk: int = 16, policy: str = "arrival"):
         self.lib = _lib.load()
+        if policy not in self.POLICIES:
+            raise ValueError(f"policy must be one of {sorted(self.POLICIES)}")
         cfg = ServerConfig(int(device), float(hbm_budget or 0.0), int(max_jobs),
-                           int(chunk))
+                           int(chunk), self.POLICIES[policy])
         self.device = int(device)
         self.h = self.lib.fa2cu_server_open(C.byref(cfg))
         if not self.h:

@@ -168,9 +168,10 @@ int fa2cu_batch_tune(int device, int use_double, int *exact_below,
  * estimated device footprint of the resident jobs stays within the budget
  * and fewer than max_jobs are resident; a scheduling thread interleaves the
  * jobs' iterations, `chunk` at a time, each job on a stream of its own
- * whose priority rises as its work (nodes x iterations) falls. A job's
- * result is the same as the single-layout path's for its inputs, whatever
- * else runs beside it. */
+ * whose priority rises as its work (nodes x iterations) falls. Jobs are
+ * admitted in arrival order, or least work first. A job's result is the
+ * same as the single-layout path's for its inputs, whatever else runs beside
+ * it. */
 typedef struct fa2cu_server fa2cu_server;
 
 typedef struct {
@@ -179,7 +180,12 @@ typedef struct {
                           device's free memory at open */
     int max_jobs;      /* jobs resident at once; <= 0: 16 */
     int chunk;         /* iterations enqueued per job at a time; <= 0: 16 */
+    int policy;        /* admission order: FA2CU_ADMIT_ARRIVAL (0) or
+                          FA2CU_ADMIT_LEAST_WORK (1: the queued job of least
+                          nodes x iterations first) */
 } fa2cu_server_config;
+
+enum { FA2CU_ADMIT_ARRIVAL = 0, FA2CU_ADMIT_LEAST_WORK = 1 };
 
 fa2cu_server *fa2cu_server_open(const fa2cu_server_config *cfg);
 

@@ -173,3 +173,21 @@ def test_footprint_matches_allocation(gpu):
                 ninc = int(g.inc_off[-1])
                 staging = max(g.n, ninc) * 8 + ninc * 4
                 assert footprint(g.n, ninc, adjust, False, prec, rep) == held + staging
+
+
+def test_server_least_work_first(gpu):
+    """With one resident job at a time and the least-work policy, jobs queued
+    behind a running one are admitted smallest first; results are unchanged."""
+    big, bpos = job("sbm", 60000, 41)
+    small = [job("ba", 2000, 42 + k) for k in range(3)]
+    want_big = single(big, bpos, 40, "single", REPULSION_BH)
+    with Server(max_jobs=1, chunk=4, policy="least_work") as S:
+        blocker = S.submit(big, bpos, 200)  # resident while the others queue
+        ids = [S.submit(big, bpos, 40)] + [S.submit(g, p, 40) for g, p in small]
+        S.wait(blocker)
+        res = {jid: S.wait(jid) for jid in ids}
+    order = sorted(ids, key=lambda j: res[j][2]["t_resident"])
+    assert order[-1] == ids[0], order  # the big job last
+    np.testing.assert_array_equal(res[ids[0]][1], want_big)
+    with pytest.raises(ValueError):
+        Server(policy="random")
