@@ -79,26 +79,14 @@ template <class T> __device__ __forceinline__ T warp_sum(T v)
 // ---- 1. bounding box (pipeline.cl:61-99) ----------------------------------
 // Block partial minima / maxima, then the last block to finish reduces the
 // partials: min and max are exact, so the result does not depend on order.
+// The end of a bounding-box pass, by every thread of a block with its
+// partial minima / maxima: the block's partial, then the last block to
+// finish reduces the partials (min and max are exact: the result does not
+// depend on order) and writes the box and the Morton quantisation.
 template <class R>
-__global__ void __launch_bounds__(256)
-k_bbox(int n, const typename RT<R>::R2 *__restrict__ pos, R *__restrict__ partial,
-       R *__restrict__ bbox, double *__restrict__ quant, unsigned *__restrict__ ticket)
+__device__ __forceinline__ void bbox_finish(R mnx, R mny, R mxx, R mxy, R *partial, R *bbox,
+                                            double *quant, unsigned *ticket)
 {
-    typedef typename RT<R>::R2 R2;
-    R mnx, mny, mxx, mxy;
-    {
-        const R2 p0 = pos[0];
-        mnx = mxx = p0.x;
-        mny = mxy = p0.y;
-    }
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n;
-         i += gridDim.x * blockDim.x) {
-        const R2 p = pos[i];
-        mnx = cl_min(mnx, p.x);
-        mny = cl_min(mny, p.y);
-        mxx = cl_max(mxx, p.x);
-        mxy = cl_max(mxy, p.y);
-    }
     for (int o = 16; o > 0; o >>= 1) {
         mnx = cl_min(mnx, __shfl_down_sync(0xffffffffu, mnx, o));
         mny = cl_min(mny, __shfl_down_sync(0xffffffffu, mny, o));
@@ -184,6 +172,29 @@ k_bbox(int n, const typename RT<R>::R2 *__restrict__ pos, R *__restrict__ partia
         qf[3] = b;
         *ticket = 0u;
     }
+}
+
+template <class R>
+__global__ void __launch_bounds__(256)
+k_bbox(int n, const typename RT<R>::R2 *__restrict__ pos, R *__restrict__ partial,
+       R *__restrict__ bbox, double *__restrict__ quant, unsigned *__restrict__ ticket)
+{
+    typedef typename RT<R>::R2 R2;
+    R mnx, mny, mxx, mxy;
+    {
+        const R2 p0 = pos[0];
+        mnx = mxx = p0.x;
+        mny = mxy = p0.y;
+    }
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += gridDim.x * blockDim.x) {
+        const R2 p = pos[i];
+        mnx = cl_min(mnx, p.x);
+        mny = cl_min(mny, p.y);
+        mxx = cl_max(mxx, p.x);
+        mxy = cl_max(mxy, p.y);
+    }
+    bbox_finish<R>(mnx, mny, mxx, mxy, partial, bbox, quant, ticket);
 }
 
 // ---- 2. Morton codes (pipeline.cl:105-130) ---------------------------------
@@ -1120,36 +1131,55 @@ k_swing(int n, const typename RT<R>::R2 *__restrict__ f,
 
 // ---- 8. displacement (pipeline.cl:476-506) ---------------------------------
 
+// The displacement (reference src/forceatlas2.c:780-802), fused with the
+// bounding box of the new positions that the next iteration's Morton codes
+// need: a grid-stride pass (the bounding box's block count) that moves every
+// node that may move and folds every node's position into the block's
+// minima / maxima, then bbox_finish (skipped when partial is null: exact
+// layouts need no box). Once the layout has stopped on an error, positions
+// are kept (the box is still computed).
 template <class R>
 __global__ void __launch_bounds__(256)
 k_apply(int n, int adjust, const typename RT<R>::R2 *__restrict__ f,
         typename RT<R>::R2 *__restrict__ fold, const R *__restrict__ sw,
         const uint8_t *__restrict__ fixed, typename RT<R>::R2 *__restrict__ pos,
-        const SpeedState *__restrict__ st, const int *__restrict__ status)
+        const SpeedState *__restrict__ st, const int *__restrict__ status,
+        R *__restrict__ partial, R *__restrict__ bbox, double *__restrict__ quant,
+        unsigned *__restrict__ ticket)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    if (status[ST_ERROR]) return; // the layout stopped: keep every position
+    const bool stopped = status[ST_ERROR] != 0;
     const R speed = (R) st->speed;
-    const typename RT<R>::R2 a = f[i];
-    fold[i] = a;
-    if (fixed && fixed[i]) return;
-    R factor;
-    if (adjust) {
-        const R df = fsqrt(a.x * a.x + a.y * a.y);
-        factor = fdiv(R(0.1) * speed, R(1) + fsqrt(speed * sw[i]));
-        if (df > R(0)) {
-            if (factor * df > R(10)) factor = fdiv(R(10), df);
-        } else {
-            factor = R(0);
+    R mnx = (R) INFINITY, mny = (R) INFINITY, mxx = -(R) INFINITY, mxy = -(R) INFINITY;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        typename RT<R>::R2 p = pos[i];
+        if (!stopped) {
+            const typename RT<R>::R2 a = f[i];
+            fold[i] = a;
+            if (!(fixed && fixed[i])) {
+                R factor;
+                if (adjust) {
+                    const R df = fsqrt(a.x * a.x + a.y * a.y);
+                    factor = fdiv(R(0.1) * speed, R(1) + fsqrt(speed * sw[i]));
+                    if (df > R(0)) {
+                        if (factor * df > R(10)) factor = fdiv(R(10), df);
+                    } else {
+                        factor = R(0);
+                    }
+                } else {
+                    factor = fdiv(speed, R(1) + fsqrt(speed * sw[i]));
+                }
+                p.x += a.x * factor;
+                p.y += a.y * factor;
+                pos[i] = p;
+            }
         }
-    } else {
-        factor = fdiv(speed, R(1) + fsqrt(speed * sw[i]));
+        mnx = cl_min(mnx, p.x);
+        mny = cl_min(mny, p.y);
+        mxx = cl_max(mxx, p.x);
+        mxy = cl_max(mxy, p.y);
     }
-    typename RT<R>::R2 p = pos[i];
-    p.x += a.x * factor;
-    p.y += a.y * factor;
-    pos[i] = p;
+    if (partial) // (uniform: a layout without a tree has no box to keep)
+        bbox_finish<R>(mnx, mny, mxx, mxy, partial, bbox, quant, ticket);
 }
 
 // ---- conversions between the host's doubles and the device layout --------

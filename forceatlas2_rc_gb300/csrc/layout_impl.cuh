@@ -299,9 +299,12 @@ template <class R> struct Layout : LayoutBase {
                 return 1;
             }
         }
-        if (set_positions(xy0)) return 1;
+        // status words (error flags, arrival tickets) and the previous
+        // forces start at zero; then the positions (and their bounding box,
+        // whose reduction takes a ticket)
         FA2_TRY(cudaMemsetAsync(fold, 0, (size_t) n * sizeof(R2), s), "cudaMemset", 1);
         FA2_TRY(cudaMemsetAsync(status, 0, ST_COUNT * sizeof(int), s), "cudaMemset", 1);
+        if (set_positions(xy0)) return 1;
         SpeedState h{};
         h.speed = 1.0;
         h.efficiency = 1.0;
@@ -326,10 +329,16 @@ template <class R> struct Layout : LayoutBase {
     static constexpr int EXACT_IPT = sizeof(R) == 4 ? FA2_EXACT_IPT_F32 : 1;
 
     // ---- the steps of one iteration ----
-    void launch_build()
+    // The bounding box and Morton quantisation of the current positions (the
+    // displacement computes them for the positions it writes; this is for
+    // positions set from outside).
+    void launch_bbox()
     {
         k_bbox<R><<<nbbox, 256, 0, s>>>(n, pos, bbox_partial, bbox, quant,
                                         (unsigned *) (status + ST_TICKET_BBOX));
+    }
+    void launch_build()
+    {
         k_morton<R><<<ceil_div(n, 256), 256, 0, s>>>(n, pos, quant, key, order);
     }
     void launch_sort() { sort_pairs(s, n, key, order, ss); }
@@ -397,8 +406,12 @@ template <class R> struct Layout : LayoutBase {
     {
         k_swing<R><<<nswing, 256, 0, s>>>(n, f, fold, mass, fixed, sw, trac, swing_partial,
                                           (unsigned *) (status + ST_TICKET_SWING), st, status);
-        k_apply<R><<<ceil_div(n, 256), 256, 0, s>>>(n, adjust, f, fold, sw, fixed, pos, st,
-                                                    status);
+        // with a tree, the bounding box's block count (its partials); else
+        // one thread per node
+        const int nb = bbox_partial ? nbbox : ceil_div(n, 256);
+        k_apply<R><<<nb, 256, 0, s>>>(n, adjust, f, fold, sw, fixed, pos, st, status,
+                                      bbox_partial, bbox, quant,
+                                      (unsigned *) (status + ST_TICKET_BBOX));
     }
     void launch_forces()
     {
@@ -488,6 +501,7 @@ template <class R> struct Layout : LayoutBase {
                                 cudaMemcpyHostToDevice, s),
                 "could not send the positions to the device", 1);
         k_pos_in<R><<<ceil_div(n, 256), 256, 0, s>>>(n, xy, pos);
+        if (bbox_partial) launch_bbox();
         FA2_TRY(cudaStreamSynchronize(s), "could not send the positions to the device", 1);
         return 0;
     }
