@@ -9,6 +9,7 @@
 #pragma once
 
 #include "common.cuh"
+#include "karras.cuh"
 
 namespace fa2cu {
 
@@ -284,6 +285,30 @@ k_gather(int n, int adjust, const uint32_t *__restrict__ order,
 {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
+    const uint32_t i = order[k];
+    if (i >= (uint32_t) n) { // never for a valid sort
+        atomicOr(status + ST_ERROR, ERR_BOUNDS);
+        psort[k] = mk4<R>(R(0), R(0), R(0), R(0));
+        return;
+    }
+    const typename RT<R>::R2 p = pos[i];
+    psort[k] = mk4<R>(p.x, p.y, mass[i], adjust ? size[i] : R(0));
+}
+
+// The gather and the Karras tree in one launch: thread k writes sorted
+// node k's record and builds region k (both read only the sort's output).
+template <class R>
+__global__ void __launch_bounds__(256)
+k_gather_karras(int n, int adjust, const uint32_t *__restrict__ order,
+                const typename RT<R>::R2 *__restrict__ pos, const R *__restrict__ mass,
+                const R *__restrict__ size, typename RT<R>::R4 *__restrict__ psort,
+                const uint32_t *__restrict__ key, int2 *__restrict__ child,
+                int2 *__restrict__ range, int *__restrict__ parent, int *__restrict__ rope,
+                int *__restrict__ visits, int *__restrict__ status)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    if (k < n - 1) karras_one<true>(k, n, key, child, range, parent, rope, visits);
     const uint32_t i = order[k];
     if (i >= (uint32_t) n) { // never for a valid sort
         atomicOr(status + ST_ERROR, ERR_BOUNDS);

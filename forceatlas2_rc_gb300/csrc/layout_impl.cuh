@@ -344,9 +344,9 @@ template <class R> struct Layout : LayoutBase {
     void launch_sort() { sort_pairs(s, n, key, order, ss); }
     void launch_tree()
     {
-        k_gather<R><<<ceil_div(n, 256), 256, 0, s>>>(n, adjust, order, pos, mass, size, psort,
-                                                     status);
-        karras_tree(s, n, key, child, range, parent, rope, visits);
+        k_gather_karras<R><<<ceil_div(n, 256), 256, 0, s>>>(n, adjust, order, pos, mass, size,
+                                                            psort, key, child, range, parent,
+                                                            rope, visits, status);
         k_aggregate<R><<<ceil_div(n, 256), 256, 0, s>>>(n, psort, child, parent, range, rope,
                                                         visits, agg, nodes, status);
     }
