@@ -274,26 +274,7 @@ k_morton(int n, const typename RT<R>::R2 *__restrict__ pos, const double *__rest
     idx[i] = (uint32_t) i;
 }
 
-// ---- 4a. nodes in sorted order (pipeline.cl:195-207) -----------------------
-
-template <class R>
-__global__ void __launch_bounds__(256)
-k_gather(int n, int adjust, const uint32_t *__restrict__ order,
-         const typename RT<R>::R2 *__restrict__ pos, const R *__restrict__ mass,
-         const R *__restrict__ size, typename RT<R>::R4 *__restrict__ psort,
-         int *__restrict__ status)
-{
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= n) return;
-    const uint32_t i = order[k];
-    if (i >= (uint32_t) n) { // never for a valid sort
-        atomicOr(status + ST_ERROR, ERR_BOUNDS);
-        psort[k] = mk4<R>(R(0), R(0), R(0), R(0));
-        return;
-    }
-    const typename RT<R>::R2 p = pos[i];
-    psort[k] = mk4<R>(p.x, p.y, mass[i], adjust ? size[i] : R(0));
-}
+// ---- 4a. nodes in sorted order and the Karras tree (pipeline.cl:195-270) ----
 
 // The gather and the Karras tree in one launch: thread k writes sorted
 // node k's record and builds region k (both read only the sort's output).

@@ -1,5 +1,4 @@
-// sort_tree.cu -- stable LSD radix sort of (Morton key, node index) pairs and
-// the Karras binary radix tree over the sorted keys.
+// sort_tree.cu -- stable LSD radix sort of (Morton key, node index) pairs.
 //
 // Sort (reference pipeline.cl:132-188 / src/gpu_full.c:419-435, four passes
 // of 8 bits; any stable sort gives the reference's order, ties by index):
@@ -16,7 +15,6 @@
 #include <algorithm>
 
 #include "sort_tree.cuh"
-#include "karras.cuh"
 
 namespace fa2cu {
 
@@ -316,23 +314,6 @@ void sort_pairs(cudaStream_t s, int n, uint32_t *key, uint32_t *val, const SortS
 {
     uint32_t *k = nullptr, *v = nullptr;
     sort_pairs_passes(s, n, key, val, w, 4, &k, &v); // four passes: back in key / val
-}
-
-// ---- Karras tree (pipeline.cl:209-270) -------------------------------------
-
-__global__ void __launch_bounds__(256)
-k_karras(int n, const uint32_t *__restrict__ key, int2 *__restrict__ child,
-         int2 *__restrict__ range, int *__restrict__ parent, int *__restrict__ rope,
-         int *__restrict__ visits)
-{
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n - 1) karras_one<true>(i, n, key, child, range, parent, rope, visits);
-}
-
-void karras_tree(cudaStream_t s, int n, const uint32_t *key, int2 *child, int2 *range,
-                 int *parent, int *rope, int *visits)
-{
-    k_karras<<<ceil_div(n - 1, 256), 256, 0, s>>>(n, key, child, range, parent, rope, visits);
 }
 
 } // namespace fa2cu

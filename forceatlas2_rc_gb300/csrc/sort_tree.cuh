@@ -1,6 +1,6 @@
-// sort_tree.cuh -- precision-independent steps of the construction: the
-// stable LSD radix sort of (Morton key, node) pairs and the Karras radix tree
-// (reference inst/opencl/pipeline.cl:132-270).
+// sort_tree.cuh -- the precision-independent step of the construction: the
+// stable LSD radix sort of (Morton key, node) pairs (reference
+// inst/opencl/pipeline.cl:132-188). The Karras tree is in karras.cuh.
 //
 // The sort makes one pass over the keys for the histograms of every digit,
 // then one launch per 8-bit digit: each block ranks its tile of keys stably,
@@ -49,12 +49,5 @@ void sort_pairs(cudaStream_t s, int n, uint32_t *key, uint32_t *val,
 // or the scratch buffers.
 void sort_pairs_passes(cudaStream_t s, int n, uint32_t *key, uint32_t *val,
                        const SortScratch &w, int passes, uint32_t **kout, uint32_t **vout);
-
-// Karras tree over n >= 2 sorted keys: child[r] = (left, right),
-// range[r] = (first, last) for the n-1 regions, parent of the 2n-1 tree nodes
-// (leaves are n-1+k), rope[p] = right child of the region split after sorted
-// node p (rope[n-1] = -1), visits reset to 0.
-void karras_tree(cudaStream_t s, int n, const uint32_t *key, int2 *child, int2 *range,
-                 int *parent, int *rope, int *visits);
 
 } // namespace fa2cu
