@@ -7,12 +7,14 @@
 //   mass, size, sw      R[n]    masses, radii (adjust), swinging
 //   fixed               u8[n]   (when some node is fixed)
 //   inc_off, inc        int[n+1], {int j; R coef}[E]  symmetric CSR
-//   key, order (+ ping-pong)  u32[n] x 4, counts u32[256 * n / 4096]
+//   key, order (+ ping-pong)  u32[n] x 4, look-back words u32[4 * 256 * n / 2048]
 //   psort               R4[n]   (x, y, m, r) in Morton order
 //   child, range        int2[n-1], parent int[2n-1], rope int[n],
 //   visits              int[n-1], agg Agg<R>[n-1] (double / float-float sums),
 //                       nodes BHNode<R>[n-1]
-//   packed              R4[n]   (exact repulsion only)
+//   bbox, quant         the bounding box and Morton quantisation, computed by
+//                       the displacement of the previous iteration
+//   packed, exact_part  R4[n], R2[rows n]  (exact repulsion only)
 //   st, status          FP64 speed state, status words
 #pragma once
 
@@ -36,7 +38,6 @@ inline double now_s()
     return (double) ts.tv_sec + 1e-9 * (double) ts.tv_nsec;
 }
 
-// Device allocations of a session, released together.
 // The all-pairs repulsion of n packed records into f: k_exact over `rows`
 // source ranges (exact_rows), then their fixed-order sum when rows > 1
 // (partial holds rows * n entries).
