@@ -10,6 +10,7 @@
 
 #include "common.cuh"
 #include "karras.cuh"
+#include "sort_tree.cuh"
 
 namespace fa2cu {
 
@@ -252,26 +253,36 @@ __device__ __forceinline__ uint32_t morton_cell(float v, float m, double mn, dou
     return morton_cell((double) v, mn, scale);
 }
 
+// Morton codes and the identity order of the nodes (grid-stride). With
+// `aux` set, the same launch also makes the sort's digit histograms (its
+// histogram pass; the sort then starts with its scatter passes): launch few
+// blocks then, as each adds 4 x 256 counts to the global histograms.
 template <class R>
 __global__ void __launch_bounds__(256)
 k_morton(int n, const typename RT<R>::R2 *__restrict__ pos, const double *__restrict__ quant,
-         uint32_t *__restrict__ key, uint32_t *__restrict__ idx)
+         uint32_t *__restrict__ key, uint32_t *__restrict__ idx, uint32_t *__restrict__ aux,
+         uint32_t *__restrict__ lookback, size_t nlookback)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const double minx = quant[0], miny = quant[1], scale = quant[2];
-    const typename RT<R>::R2 p = pos[i];
-    uint32_t cx, cy;
-    if constexpr (sizeof(R) == 4) {
-        const float4 qf = *reinterpret_cast<const float4 *>(quant + 4);
-        cx = morton_cell(p.x, qf.z, minx, scale, qf.x, qf.y);
-        cy = morton_cell(p.y, qf.w, miny, scale, qf.x, qf.y);
-    } else {
-        cx = morton_cell(p.x, minx, scale);
-        cy = morton_cell(p.y, miny, scale);
+    __shared__ SortHistShared H;
+    if (aux) hist_begin(H, lookback, nlookback); // (uniform)
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const double minx = quant[0], miny = quant[1], scale = quant[2];
+        const typename RT<R>::R2 p = pos[i];
+        uint32_t cx, cy;
+        if constexpr (sizeof(R) == 4) {
+            const float4 qf = *reinterpret_cast<const float4 *>(quant + 4);
+            cx = morton_cell(p.x, qf.z, minx, scale, qf.x, qf.y);
+            cy = morton_cell(p.y, qf.w, miny, scale, qf.x, qf.y);
+        } else {
+            cx = morton_cell(p.x, minx, scale);
+            cy = morton_cell(p.y, miny, scale);
+        }
+        const uint32_t k = spread16(cx) | (spread16(cy) << 1);
+        key[i] = k;
+        idx[i] = (uint32_t) i;
+        if (aux) hist_add(H, k, 4);
     }
-    key[i] = spread16(cx) | (spread16(cy) << 1);
-    idx[i] = (uint32_t) i;
+    if (aux) hist_end(H, 4, aux);
 }
 
 // ---- 4a. nodes in sorted order and the Karras tree (pipeline.cl:195-270) ----

@@ -338,11 +338,15 @@ template <class R> struct Layout : LayoutBase {
         k_bbox<R><<<nbbox, 256, 0, s>>>(n, pos, bbox_partial, bbox, quant,
                                         (unsigned *) (status + ST_TICKET_BBOX));
     }
+    // Morton codes, with the sort's digit histograms in the same launch
     void launch_build()
     {
-        k_morton<R><<<ceil_div(n, 256), 256, 0, s>>>(n, pos, quant, key, order);
+        sort_prepare(s, ss);
+        const int nb = std::min(ceil_div(n, 256), 152 * 4);
+        k_morton<R><<<nb, 256, 0, s>>>(n, pos, quant, key, order, ss.digit_total, ss.counts,
+                                       sort_status_words(n, 4));
     }
-    void launch_sort() { sort_pairs(s, n, key, order, ss); }
+    void launch_sort() { sort_pairs(s, n, key, order, ss, /*hist_ready=*/true); }
     void launch_tree()
     {
         k_gather_karras<R><<<ceil_div(n, 256), 256, 0, s>>>(n, adjust, order, pos, mass, size,

@@ -94,7 +94,7 @@ extern "C" int fa2cu_morton_order_noalloc(int n, const float *pos, uint32_t *key
                                         (float *) (base + OFF_BBOX), (double *) (base + OFF_QUANT),
                                         ticket);
     k_morton<float><<<ceil_div(n, 256), 256, 0, s>>>(n, p2, (const double *) (base + OFF_QUANT),
-                                                     key, order);
+                                                     key, order, nullptr, nullptr, 0);
     if (sort_setup()) return 1;
     SortScratch w;
     w.key_b = (uint32_t *) (base + OFF_KEY_B);

@@ -25,33 +25,6 @@ __device__ __forceinline__ unsigned lanemask_lt()
     return m;
 }
 
-// Block-wide inclusive scan of one value per thread (blockDim.x <= 1024).
-__device__ __forceinline__ uint32_t block_incl_scan(uint32_t v, uint32_t *warp_tot,
-                                                    uint32_t *total)
-{
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    for (int o = 1; o < 32; o <<= 1) {
-        const uint32_t t = __shfl_up_sync(0xffffffffu, v, o);
-        if (lane >= o) v += t;
-    }
-    if (lane == 31) warp_tot[w] = v;
-    __syncthreads();
-    if (w == 0) {
-        const int nw = blockDim.x >> 5;
-        uint32_t s = lane < nw ? warp_tot[lane] : 0;
-        for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t t = __shfl_up_sync(0xffffffffu, s, o);
-            if (lane >= o) s += t;
-        }
-        if (lane < nw) warp_tot[lane] = s;
-        if (lane == nw - 1) *total = s;
-    }
-    __syncthreads();
-    const uint32_t r = v + (w > 0 ? warp_tot[w - 1] : 0);
-    __syncthreads();
-    return r;
-}
-
 // Histograms of every digit of the keys (one pass), the status words of the
 // look-back zeroed; the last block to finish turns the histograms into digit
 // bases (exclusive scans).
@@ -59,45 +32,12 @@ __global__ void __launch_bounds__(SORT_THREADS)
 k_sort_hist4(int n, int passes, const uint32_t *__restrict__ key, uint32_t *__restrict__ status,
              size_t nstatus, uint32_t *__restrict__ aux)
 {
-    // per-warp counters (shared-memory atomics, contention within a warp
-    // only), summed over the warps at the end
-    constexpr int NW = SORT_THREADS / 32;
-    __shared__ uint32_t h[NW][4][256];
-    __shared__ uint32_t wt[32];
-    __shared__ uint32_t tot;
-    __shared__ int last;
-    for (int d = threadIdx.x; d < NW * 4 * 256; d += SORT_THREADS) (&h[0][0][0])[d] = 0;
-    for (size_t i = (size_t) blockIdx.x * SORT_THREADS + threadIdx.x; i < nstatus;
-         i += (size_t) gridDim.x * SORT_THREADS)
-        status[i] = 0u;
-    __syncthreads();
-    const int w = threadIdx.x >> 5;
+    __shared__ SortHistShared S;
+    hist_begin(S, status, nstatus);
     for (int idx = blockIdx.x * SORT_THREADS + threadIdx.x; idx < n;
-         idx += gridDim.x * SORT_THREADS) {
-        const uint32_t k = key[idx];
-        for (int p = 0; p < passes; p++) atomicAdd(&h[w][p][(k >> (8 * p)) & 255u], 1u);
-    }
-    __syncthreads();
-    for (int p = 0; p < passes; p++) {
-        uint32_t c = 0;
-        for (int ww = 0; ww < NW; ww++) c += h[ww][p][threadIdx.x];
-        if (c) atomicAdd(aux + SORT_AUX_HIST + p * 256 + threadIdx.x, c);
-    }
-    __threadfence();
-    __syncthreads();
-    if (threadIdx.x == 0)
-        last = atomicAdd(aux + SORT_AUX_DONE, 1u) == gridDim.x - 1;
-    __syncthreads();
-    if (!last) return;
-    __threadfence();
-    for (int p = 0; p < passes; p++) {
-        const uint32_t c = __ldcg(aux + SORT_AUX_HIST + p * 256 + threadIdx.x);
-        const uint32_t incl = block_incl_scan(c, wt, &tot);
-        aux[SORT_AUX_BASE + p * 256 + threadIdx.x] = incl - c;
-        aux[SORT_AUX_HIST + p * 256 + threadIdx.x] = 0u;
-    }
-    if (threadIdx.x < 4) aux[SORT_AUX_TICKET + threadIdx.x] = 0u;
-    if (threadIdx.x == 0) aux[SORT_AUX_DONE] = 0u;
+         idx += gridDim.x * SORT_THREADS)
+        hist_add(S, key[idx], passes);
+    hist_end(S, passes, aux);
 }
 
 // Look-back words: the tile's count of a digit, or (once known) the count of
@@ -282,15 +222,24 @@ static void onesweep_pass(cudaStream_t s, int n, int pass, const uint32_t *kin,
 
 size_t sort_scratch_counts(int n) { return 4 * 256 * (size_t) ceil_div(n, SORT_TILE); }
 
-void sort_pairs_passes(cudaStream_t s, int n, uint32_t *key, uint32_t *val,
-                       const SortScratch &w, int passes, uint32_t **kout, uint32_t **vout)
+size_t sort_status_words(int n, int passes) { return (size_t) passes * 256 * ceil_div(n, SORT_TILE); }
+
+void sort_prepare(cudaStream_t s, const SortScratch &w)
 {
-    const int nb = ceil_div(n, SORT_TILE);
-    const int hist_blocks = std::min(nb, 152 * 4);
     // histograms, bases and tickets start at zero
     cudaMemsetAsync(w.digit_total, 0, SORT_AUX * sizeof(uint32_t), s);
-    k_sort_hist4<<<hist_blocks, SORT_THREADS, 0, s>>>(n, passes, key, w.counts,
-                                                     (size_t) passes * 256 * nb, w.digit_total);
+}
+
+void sort_pairs_passes(cudaStream_t s, int n, uint32_t *key, uint32_t *val,
+                       const SortScratch &w, int passes, uint32_t **kout, uint32_t **vout,
+                       bool hist_ready)
+{
+    if (!hist_ready) {
+        const int hist_blocks = std::min(ceil_div(n, SORT_TILE), 152 * 4);
+        sort_prepare(s, w);
+        k_sort_hist4<<<hist_blocks, SORT_THREADS, 0, s>>>(
+            n, passes, key, w.counts, sort_status_words(n, passes), w.digit_total);
+    }
     uint32_t *ka = key, *va = val, *kb = w.key_b, *vb = w.val_b;
     for (int pass = 0; pass < passes; pass++) {
         if (w.tile_threads == 1024)
@@ -310,10 +259,11 @@ void sort_pairs_passes(cudaStream_t s, int n, uint32_t *key, uint32_t *val,
     *vout = va;
 }
 
-void sort_pairs(cudaStream_t s, int n, uint32_t *key, uint32_t *val, const SortScratch &w)
+void sort_pairs(cudaStream_t s, int n, uint32_t *key, uint32_t *val, const SortScratch &w,
+                bool hist_ready)
 {
     uint32_t *k = nullptr, *v = nullptr;
-    sort_pairs_passes(s, n, key, val, w, 4, &k, &v); // four passes: back in key / val
+    sort_pairs_passes(s, n, key, val, w, 4, &k, &v, hist_ready); // four passes: back in key / val
 }
 
 } // namespace fa2cu

@@ -40,14 +40,102 @@ size_t sort_scratch_counts(int n); // entries of `counts`
 int sort_setup();
 
 // Stable sort of key/val (n pairs) by key, 4 passes of 8 bits; the result is
-// back in key / val.
+// back in key / val. hist_ready: the digit histograms were already made by
+// the kernel that produced the keys (sort_prepare, then hist_begin /
+// hist_add / hist_end there); else the sort makes them.
 void sort_pairs(cudaStream_t s, int n, uint32_t *key, uint32_t *val,
-                const SortScratch &w);
+                const SortScratch &w, bool hist_ready = false);
+
+// Clears the histograms and tickets (before the histogram pass).
+void sort_prepare(cudaStream_t s, const SortScratch &w);
+// Look-back words the histogram pass clears, for n keys and `passes` digits.
+size_t sort_status_words(int n, int passes);
+
+// Block-wide inclusive scan of one value per thread (blockDim.x <= 1024).
+__device__ __forceinline__ uint32_t block_incl_scan(uint32_t v, uint32_t *warp_tot,
+                                                    uint32_t *total)
+{
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t t = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o) v += t;
+    }
+    if (lane == 31) warp_tot[w] = v;
+    __syncthreads();
+    if (w == 0) {
+        const int nw = blockDim.x >> 5;
+        uint32_t s = lane < nw ? warp_tot[lane] : 0;
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t t = __shfl_up_sync(0xffffffffu, s, o);
+            if (lane >= o) s += t;
+        }
+        if (lane < nw) warp_tot[lane] = s;
+        if (lane == nw - 1) *total = s;
+    }
+    __syncthreads();
+    const uint32_t r = v + (w > 0 ? warp_tot[w - 1] : 0);
+    __syncthreads();
+    return r;
+}
+
+// The sort's histogram pass inside a kernel of SORT_THREADS threads per
+// block: every block calls hist_begin (clears its per-warp counters and a
+// share of the look-back words), hist_add per key it has, then hist_end (adds
+// its counts to the global ones; the last block to finish turns them into
+// digit bases). Every thread of every block must reach hist_begin and
+// hist_end.
+struct SortHistShared {
+    uint32_t h[SORT_THREADS / 32][4][256];
+    uint32_t wt[32];
+    uint32_t tot;
+    int last;
+};
+
+__device__ __forceinline__ void hist_begin(SortHistShared &S, uint32_t *status, size_t nstatus)
+{
+    for (int d = threadIdx.x; d < (SORT_THREADS / 32) * 4 * 256; d += SORT_THREADS)
+        (&S.h[0][0][0])[d] = 0;
+    for (size_t i = (size_t) blockIdx.x * SORT_THREADS + threadIdx.x; i < nstatus;
+         i += (size_t) gridDim.x * SORT_THREADS)
+        status[i] = 0u;
+    __syncthreads();
+}
+
+__device__ __forceinline__ void hist_add(SortHistShared &S, uint32_t key, int passes)
+{
+    const int w = threadIdx.x >> 5;
+    for (int p = 0; p < passes; p++) atomicAdd(&S.h[w][p][(key >> (8 * p)) & 255u], 1u);
+}
+
+__device__ __forceinline__ void hist_end(SortHistShared &S, int passes, uint32_t *aux)
+{
+    __syncthreads();
+    for (int p = 0; p < passes; p++) {
+        uint32_t c = 0;
+        for (int ww = 0; ww < SORT_THREADS / 32; ww++) c += S.h[ww][p][threadIdx.x];
+        if (c) atomicAdd(aux + SORT_AUX_HIST + p * 256 + threadIdx.x, c);
+    }
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) S.last = atomicAdd(aux + SORT_AUX_DONE, 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (!S.last) return;
+    __threadfence();
+    for (int p = 0; p < passes; p++) {
+        const uint32_t c = __ldcg(aux + SORT_AUX_HIST + p * 256 + threadIdx.x);
+        const uint32_t incl = block_incl_scan(c, S.wt, &S.tot);
+        aux[SORT_AUX_BASE + p * 256 + threadIdx.x] = incl - c;
+        aux[SORT_AUX_HIST + p * 256 + threadIdx.x] = 0u;
+    }
+    if (threadIdx.x < 4) aux[SORT_AUX_TICKET + threadIdx.x] = 0u;
+    if (threadIdx.x == 0) aux[SORT_AUX_DONE] = 0u;
+}
 
 // The same with `passes` (1..4) passes of 8 bits, for keys below
 // 2^(8 passes); the sorted pairs are left in (*kout, *vout), either key / val
 // or the scratch buffers.
 void sort_pairs_passes(cudaStream_t s, int n, uint32_t *key, uint32_t *val,
-                       const SortScratch &w, int passes, uint32_t **kout, uint32_t **vout);
+                       const SortScratch &w, int passes, uint32_t **kout, uint32_t **vout,
+                       bool hist_ready = false);
 
 } // namespace fa2cu
