@@ -45,10 +45,10 @@ WORKLOAD = ("SBM n=1,000,000, 1000 power-law blocks (exp 2.1), deg_in 12, "
             "deg_out 2, unit weights; linlog + dissuade_hubs, Barnes-Hut "
             "theta 1.2, FP32 positions/forces, FP64 speed control")
 # kernels of one Barnes-Hut iteration: morton (with the sort's histograms),
-# 4 sort scatter passes, gather + karras, aggregate, traverse, attract,
-# swing, apply (with the next iteration's bounding box), and one memset of
-# the sort's counters
-LAUNCHES_PER_ITER = 11
+# 4 sort scatter passes, gather + karras, aggregate, traverse, attraction +
+# swing totals + speed update, apply (with the next iteration's bounding
+# box), and one memset of the sort's counters
+LAUNCHES_PER_ITER = 10
 # Barnes-Hut walks (fa2cu_layout_option "walk"): identical forces
 WALKS = {"warp": 0, "thread": 1, "wide": 2, "pair": 3, "quad": 4}
 # algorithmic HBM bytes per node of the traversal: psort record 16, order 4,

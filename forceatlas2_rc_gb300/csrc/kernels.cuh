@@ -1012,75 +1012,88 @@ __device__ inline void update_speed_dev(SpeedState *st, double tsw, double ttr)
 // more than the rest of the iteration).
 constexpr int SERIAL_TOTALS_MAX = 2048;
 
+// Per-thread sums of swinging and traction over the nodes that can move:
+// float-float in the FP32 path, double in the FP64 path.
+template <class R> struct SwingAcc {
+    ff2 s = ff2{0.0f, 0.0f}, t = ff2{0.0f, 0.0f};
+    double ds = 0.0, dt = 0.0;
+};
+
+// Node i's swinging (kept for the displacement) and traction
+// (reference src/forceatlas2.c:758-775), added to the thread's sums.
 template <class R>
-__global__ void __launch_bounds__(256)
-k_swing(int n, const typename RT<R>::R2 *__restrict__ f,
-        const typename RT<R>::R2 *__restrict__ fold, const R *__restrict__ mass,
-        const uint8_t *__restrict__ fixed, R *__restrict__ sw, R *__restrict__ tr,
-        double2 *__restrict__ partial, unsigned *__restrict__ ticket,
-        SpeedState *__restrict__ st, int *__restrict__ status)
+__device__ __forceinline__ void swing_node(int i, int n, const typename RT<R>::R2 *f,
+                                           const typename RT<R>::R2 *fold, const R *mass,
+                                           const uint8_t *fixed, R *sw, R *tr, SwingAcc<R> &acc)
 {
-    // per thread: in float-float (FP32 path) or double (FP64 path), over a
-    // fixed set of nodes
-    ff2 fs = ff_from(0.0f), ft = ff_from(0.0f);
-    double as = 0.0, at = 0.0;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n;
-         i += gridDim.x * blockDim.x) {
-        const typename RT<R>::R2 a = f[i], b = fold[i];
-        const R sx = b.x - a.x, sy = b.y - a.y;
-        const R tx = b.x + a.x, ty = b.y + a.y;
-        const R m = mass[i];
-        const R s = m * fsqrt(sx * sx + sy * sy);
-        const R t = R(0.5) * m * fsqrt(tx * tx + ty * ty);
-        sw[i] = s;
-        if (n <= SERIAL_TOTALS_MAX) tr[i] = t;
-        if (fixed && fixed[i]) continue;
-        if constexpr (sizeof(R) == 4) {
-            fs = ff_add(fs, ff_from((float) s));
-            ft = ff_add(ft, ff_from((float) t));
-        } else {
-            as = __dadd_rn(as, (double) s);
-            at = __dadd_rn(at, (double) t);
-        }
+    const typename RT<R>::R2 a = f[i], b = fold[i];
+    const R sx = b.x - a.x, sy = b.y - a.y;
+    const R tx = b.x + a.x, ty = b.y + a.y;
+    const R m = mass[i];
+    const R s = m * fsqrt(sx * sx + sy * sy);
+    const R t = R(0.5) * m * fsqrt(tx * tx + ty * ty);
+    sw[i] = s;
+    if (n <= SERIAL_TOTALS_MAX) tr[i] = t;
+    if (fixed && fixed[i]) return;
+    if constexpr (sizeof(R) == 4) {
+        acc.s = ff_add(acc.s, ff_from((float) s));
+        acc.t = ff_add(acc.t, ff_from((float) t));
+    } else {
+        acc.ds = __dadd_rn(acc.ds, (double) s);
+        acc.dt = __dadd_rn(acc.dt, (double) t);
     }
-    // per warp and per block, in a fixed tree order: float-float in the FP32
-    // path (one conversion to double per block), double with compensation
-    // in the FP64 path
-    __shared__ double ss[8], st_[8];
-    __shared__ ff2 fss[8], fst[8];
+}
+
+__device__ __forceinline__ ff2 ff_shfl_down(ff2 a, int o)
+{
+    return ff2{__shfl_down_sync(0xffffffffu, a.hi, o), __shfl_down_sync(0xffffffffu, a.lo, o)};
+}
+
+// The end of the totals, by every thread of every block of the kernel: the
+// block's sums in a fixed tree order (float-float or compensated double), a
+// partial per block, then the last block to finish sums the partials in a
+// fixed order (float-float in the FP32 path, the partials' pairs being
+// (hi, lo) floats; compensated double in the FP64 path) -- or, up to
+// SERIAL_TOTALS_MAX nodes, sums the nodes serially in node order in double
+// (the reference's order) -- and updates Gephi's adaptive speed in double.
+template <class R>
+__device__ __forceinline__ void swing_finish(SwingAcc<R> acc, int n, const uint8_t *fixed,
+                                             const R *sw, const R *tr, double2 *partial,
+                                             unsigned *ticket, SpeedState *st, int *status)
+{
+    __shared__ double ss[32], st_[32];
+    __shared__ ff2 fss[32], fst[32];
     __shared__ int last;
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
     if constexpr (sizeof(R) == 4) {
         for (int o = 16; o > 0; o >>= 1) {
-            fs = ff_add(fs, ff2{__shfl_down_sync(0xffffffffu, fs.hi, o),
-                                __shfl_down_sync(0xffffffffu, fs.lo, o)});
-            ft = ff_add(ft, ff2{__shfl_down_sync(0xffffffffu, ft.hi, o),
-                                __shfl_down_sync(0xffffffffu, ft.lo, o)});
+            acc.s = ff_add(acc.s, ff_shfl_down(acc.s, o));
+            acc.t = ff_add(acc.t, ff_shfl_down(acc.t, o));
         }
         if (lane == 0) {
-            fss[w] = fs;
-            fst[w] = ft;
+            fss[w] = acc.s;
+            fst[w] = acc.t;
         }
     } else {
-        as = warp_sum(as);
-        at = warp_sum(at);
+        acc.ds = warp_sum(acc.ds);
+        acc.dt = warp_sum(acc.dt);
         if (lane == 0) {
-            ss[w] = as;
-            st_[w] = at;
+            ss[w] = acc.ds;
+            st_[w] = acc.dt;
         }
     }
     __syncthreads();
     if (threadIdx.x == 0) {
         if constexpr (sizeof(R) == 4) {
             ff2 a = fss[0], b = fst[0];
-            for (int k = 1; k < (int) (blockDim.x >> 5); k++) {
+            for (int k = 1; k < nw; k++) {
                 a = ff_add(a, fss[k]);
                 b = ff_add(b, fst[k]);
             }
-            partial[blockIdx.x] = make_double2(ff_to_double(a), ff_to_double(b));
+            reinterpret_cast<float4 *>(partial)[blockIdx.x] = make_float4(a.hi, a.lo, b.hi, b.lo);
         } else {
             double a = 0.0, b = 0.0, ca = 0.0, cb = 0.0;
-            for (int k = 0; k < (int) (blockDim.x >> 5); k++) {
+            for (int k = 0; k < nw; k++) {
                 neumaier(a, ca, ss[k]);
                 neumaier(b, cb, st_[k]);
             }
@@ -1092,49 +1105,69 @@ k_swing(int n, const typename RT<R>::R2 *__restrict__ f,
     __syncthreads();
     if (!last) return;
     __threadfence();
+    double tsw = 0.0, ttr = 0.0;
     if (n <= SERIAL_TOTALS_MAX) {
         if (threadIdx.x == 0) {
-            double tsw = 0.0, ttr = 0.0;
             for (int i = 0; i < n; i++) {
                 if (fixed && fixed[i]) continue;
                 tsw = __dadd_rn(tsw, (double) __ldcg(sw + i));
                 ttr = __dadd_rn(ttr, (double) __ldcg(tr + i));
             }
-            *ticket = 0u;
-            if (!(tsw == tsw) || !(ttr == ttr)) {
-                atomicOr(status + ST_ERROR, ERR_NAN);
-                st->total_swinging = tsw;
-                st->total_traction = ttr;
-            } else {
-                update_speed_dev(st, tsw, ttr);
+        }
+    } else if constexpr (sizeof(R) == 4) {
+        // the partials: per thread (strided, fixed), per warp, over the warps
+        ff2 a = ff2{0.0f, 0.0f}, b = ff2{0.0f, 0.0f};
+        const float4 *pf = reinterpret_cast<const float4 *>(partial);
+        for (int k = threadIdx.x; k < (int) gridDim.x; k += blockDim.x) {
+            const float4 v = __ldcg(pf + k);
+            a = ff_add(a, ff2{v.x, v.y});
+            b = ff_add(b, ff2{v.z, v.w});
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            a = ff_add(a, ff_shfl_down(a, o));
+            b = ff_add(b, ff_shfl_down(b, o));
+        }
+        __syncthreads();
+        if (lane == 0) {
+            fss[w] = a;
+            fst[w] = b;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            a = fss[0];
+            b = fst[0];
+            for (int k = 1; k < nw; k++) {
+                a = ff_add(a, fss[k]);
+                b = ff_add(b, fst[k]);
             }
+            tsw = ff_to_double(a);
+            ttr = ff_to_double(b);
         }
-        return;
+    } else {
+        double s1 = 0.0, c1 = 0.0, s2 = 0.0, c2 = 0.0;
+        for (int k = threadIdx.x; k < (int) gridDim.x; k += blockDim.x) {
+            const double2 v = __ldcg(partial + k);
+            neumaier(s1, c1, v.x);
+            neumaier(s2, c2, v.y);
+        }
+        double v1 = warp_sum(__dadd_rn(s1, c1)), v2 = warp_sum(__dadd_rn(s2, c2));
+        __syncthreads();
+        if (lane == 0) {
+            ss[w] = v1;
+            st_[w] = v2;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double t1 = 0.0, k1 = 0.0, t2 = 0.0, k2 = 0.0;
+            for (int k = 0; k < nw; k++) {
+                neumaier(t1, k1, ss[k]);
+                neumaier(t2, k2, st_[k]);
+            }
+            tsw = __dadd_rn(t1, k1);
+            ttr = __dadd_rn(t2, k2);
+        }
     }
-    // the block partials: compensated per thread (strided, fixed), then a
-    // fixed tree over the threads
-    double s1 = 0.0, c1 = 0.0, s2 = 0.0, c2 = 0.0;
-    for (int k = threadIdx.x; k < (int) gridDim.x; k += blockDim.x) {
-        const double2 v = __ldcg(partial + k);
-        neumaier(s1, c1, v.x);
-        neumaier(s2, c2, v.y);
-    }
-    double v1 = __dadd_rn(s1, c1), v2 = __dadd_rn(s2, c2);
-    v1 = warp_sum(v1);
-    v2 = warp_sum(v2);
-    __syncthreads();
-    if (lane == 0) {
-        ss[w] = v1;
-        st_[w] = v2;
-    }
-    __syncthreads();
     if (threadIdx.x == 0) {
-        double t1 = 0.0, k1 = 0.0, t2 = 0.0, k2 = 0.0;
-        for (int k = 0; k < (int) (blockDim.x >> 5); k++) {
-            neumaier(t1, k1, ss[k]);
-            neumaier(t2, k2, st_[k]);
-        }
-        const double tsw = __dadd_rn(t1, k1), ttr = __dadd_rn(t2, k2);
         *ticket = 0u;
         if (!(tsw == tsw) || !(ttr == ttr)) {
             atomicOr(status + ST_ERROR, ERR_NAN);
@@ -1144,6 +1177,29 @@ k_swing(int n, const typename RT<R>::R2 *__restrict__ f,
             update_speed_dev(st, tsw, ttr);
         }
     }
+}
+
+// Attraction and gravity, then (the node's force complete) its swinging and
+// traction, and the totals with the speed update: one thread per node, one
+// launch for the attraction and the totals.
+template <class R>
+__global__ void __launch_bounds__(256)
+k_attract_swing(int n, R gravity, int strong, int linlog, int adjust,
+                const typename RT<R>::R2 *__restrict__ pos, const R *__restrict__ mass,
+                const R *__restrict__ size, const int *__restrict__ off,
+                const Inc<R> *__restrict__ inc, typename RT<R>::R2 *__restrict__ f,
+                const typename RT<R>::R2 *__restrict__ fold, const uint8_t *__restrict__ fixed,
+                R *__restrict__ sw, R *__restrict__ tr, double2 *__restrict__ partial,
+                unsigned *__restrict__ ticket, SpeedState *__restrict__ st,
+                int *__restrict__ status)
+{
+    SwingAcc<R> acc;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) {
+        attract_one<R>(i, gravity, strong, linlog, adjust, pos, mass, size, off, inc, f);
+        swing_node<R>(i, n, f, fold, mass, fixed, sw, tr, acc);
+    }
+    swing_finish<R>(acc, n, fixed, sw, tr, partial, ticket, st, status);
 }
 
 // ---- 8. displacement (pipeline.cl:476-506) ---------------------------------

@@ -78,7 +78,7 @@ template <class R> struct Layout : LayoutBase {
     Inc<R> *inc = nullptr;
     R *bbox = nullptr, *bbox_partial = nullptr;
     double *quant = nullptr; // min x, min y, Morton scale, -, 4 floats (k_bbox)
-    int nbbox = 1, nswing = 1;
+    int nbbox = 1;
     uint32_t *key = nullptr, *order = nullptr;
     SortScratch ss{};
     R4 *psort = nullptr, *packed = nullptr;
@@ -123,8 +123,7 @@ template <class R> struct Layout : LayoutBase {
         fixed = any_fixed ? mem.get<uint8_t>(nn) : nullptr;
         inc_off = mem.get<int>(nn + 1);
         inc = mem.get<Inc<R>>((size_t) ninc);
-        nswing = std::min(ceil_div(n, 256), 152 * 2);
-        swing_partial = mem.get<double2>((size_t) nswing);
+        swing_partial = mem.get<double2>((size_t) ceil_div(n, 256)); // one per block
         st = mem.get<SpeedState>(1);
         status = mem.get<int>(ST_COUNT);
         xy = mem.get<double>(2 * nn);
@@ -402,15 +401,23 @@ template <class R> struct Layout : LayoutBase {
                                        status);
         }
     }
+    // Attraction and gravity only (the forces of fa2cu_layout_forces).
     void launch_attraction()
     {
         k_attract<R><<<ceil_div(n, 256), 256, 0, s>>>(n, gravity, strong, linlog, adjust, pos,
                                                       mass, size, inc_off, inc, f);
     }
+    // Attraction and gravity, swinging, traction, the totals and the speed
+    // update (an iteration's second half before the displacement).
+    void launch_attraction_swing()
+    {
+        k_attract_swing<R><<<ceil_div(n, 256), 256, 0, s>>>(
+            n, gravity, strong, linlog, adjust, pos, mass, size, inc_off, inc, f, fold, fixed, sw,
+            trac, swing_partial, (unsigned *) (status + ST_TICKET_SWING), st, status);
+    }
+    // The displacement, with the next iteration's bounding box.
     void launch_move()
     {
-        k_swing<R><<<nswing, 256, 0, s>>>(n, f, fold, mass, fixed, sw, trac, swing_partial,
-                                          (unsigned *) (status + ST_TICKET_SWING), st, status);
         // with a tree, the bounding box's block count (its partials); else
         // one thread per node
         const int nb = bbox_partial ? nbbox : ceil_div(n, 256);
@@ -418,7 +425,7 @@ template <class R> struct Layout : LayoutBase {
                                       bbox_partial, bbox, quant,
                                       (unsigned *) (status + ST_TICKET_BBOX));
     }
-    void launch_forces()
+    void launch_repel()
     {
         if (repulsion == FA2CU_REPULSION_BH) {
             launch_build();
@@ -426,11 +433,16 @@ template <class R> struct Layout : LayoutBase {
             launch_tree();
         }
         launch_repulsion();
+    }
+    void launch_forces()
+    {
+        launch_repel();
         launch_attraction();
     }
     void launch_iteration()
     {
-        launch_forces();
+        launch_repel();
+        launch_attraction_swing();
         launch_move();
     }
 
@@ -555,7 +567,7 @@ template <class R> struct Layout : LayoutBase {
             }
             launch_repulsion();
             cudaEventRecord(ev[e++], s);
-            launch_attraction();
+            launch_attraction_swing(); // "attraction": with the totals and speed
             cudaEventRecord(ev[e++], s);
             launch_move();
             cudaEventRecord(ev[e++], s);
