@@ -94,7 +94,11 @@ def edge_weights(m, weights, edge_weight_influence=1.0, normalize_weights=False,
     if weights is None:
         w = np.ones(m)
     else:
-        w = np.asarray(weights, dtype=np.float64).reshape(-1)
+        try:
+            w = np.asarray(weights, dtype=np.float64).reshape(-1)
+        except (TypeError, ValueError):
+            raise ValueError("`weights` must be a numeric vector with one value "
+                             f"per edge ({m}).") from None
         if w.size != m:
             raise ValueError(f"`weights` must have one value per edge ({m}), "
                              f"not {w.size}.")
@@ -107,7 +111,8 @@ def edge_weights(m, weights, edge_weight_influence=1.0, normalize_weights=False,
     if normalize_weights and m > 0:
         lo, hi = w.min(), w.max()
         w = (w - lo) / (hi - lo) if lo < hi else np.ones(m)
-    w = np.ones(m) if edge_weight_influence == 0 else w ** edge_weight_influence
+    with np.errstate(over="ignore"):
+        w = np.ones(m) if edge_weight_influence == 0 else w ** edge_weight_influence
     if (~np.isfinite(w)).any():
         raise ValueError("The edge weights are too large or too small to be used.")
     return w
@@ -358,11 +363,15 @@ def _common(n, edges, iterations, scaling_ratio, gravity, jitter_tolerance,
         scaling_ratio = 2.0 if n >= 100 else 10.0
     else:
         scaling_ratio = _number(scaling_ratio, "scaling_ratio", 0, strict=True)
-    size = np.broadcast_to(np.asarray(node_size, dtype=np.float64), (n,)).copy() \
-        if np.ndim(node_size) == 0 else np.asarray(node_size, dtype=np.float64)
+    size_err = (f"`node_size` must be a single number or one finite number "
+                f"per node ({n}).")
+    try:
+        size = np.broadcast_to(np.asarray(node_size, dtype=np.float64), (n,)).copy() \
+            if np.ndim(node_size) == 0 else np.asarray(node_size, dtype=np.float64)
+    except (TypeError, ValueError):
+        raise ValueError(size_err) from None
     if size.shape != (n,) or (~np.isfinite(size)).any():
-        raise ValueError(f"`node_size` must be a single number or one finite "
-                         f"number per node ({n}).")
+        raise ValueError(size_err)
     if (size < 0).any():
         raise ValueError("`node_size` must be non-negative.")
     if fixed is None:
