@@ -56,7 +56,7 @@ WALKS = {"warp": 0, "thread": 1, "wide": 2, "pair": 3, "quad": 4}
 TRAVERSE_HBM_BYTES_PER_NODE = 28
 # DRAM bytes (read + write) of one traversal launch on this workload, from
 # one ncu capture (profiles/kernels_sbm1m_full.md)
-TRAVERSE_DRAM_BYTES = 48.21e6 + 0.73e6
+TRAVERSE_DRAM_BYTES = 48.20e6 + 0.66e6
 
 
 def make_workload(small: bool = False):
@@ -78,30 +78,109 @@ def dist_env():
 
 
 class Clocks:
-    """nvidia-smi samples of SM clocks and throttle reasons while running."""
+    """SM clock and clock-event (throttle) reasons sampled while the timed
+    region runs: NVML read every 5 ms from a host thread (a 50-iteration
+    region lasts ~50 ms), else `nvidia-smi -lms 200`. Only reads the GPU's
+    state. `__enter__` returns once the first sample is in, so the samples
+    cover the region that follows."""
     FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,"
               "clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,"
               "clocks_event_reasons.sw_power_cap")
+    # nvmlClocksEventReasons bits (nvml.h): SW power cap, HW slowdown, SW
+    # thermal, HW thermal
+    NVML_BITS = {"sw_power_cap": 0x4, "hw_slowdown": 0x8,
+                 "sw_thermal_slowdown": 0x20, "hw_thermal_slowdown": 0x40}
+    NVML_CLOCK_SM = 1
 
     def __init__(self, device: int):
         self.dev = device
         self.proc = None
         self.f = None
+        self.nvml = None
+        self.handle = None
+        self.rows = []
+        self.stop = None
+        self.thread = None
+        self.source = None
+
+    def _nvml_handle(self):
+        import ctypes as C
+        try:
+            lib = C.CDLL("libnvidia-ml.so.1")
+            if lib.nvmlInit_v2() != 0:
+                return False
+        except Exception:
+            return False
+        h = C.c_void_p()
+        try:
+            import torch
+            pr = torch.cuda.get_device_properties(self.dev)
+            bus = f"{pr.pci_domain_id:08x}:{pr.pci_bus_id:02x}:{pr.pci_device_id:02x}.0"
+            rc = lib.nvmlDeviceGetHandleByPciBusId_v2(bus.encode(), C.byref(h))
+        except Exception:
+            rc = -1
+        if rc != 0:
+            visible = os.environ.get("CUDA_VISIBLE_DEVICES", "")
+            if visible and "," not in visible and visible.strip().isdigit():
+                idx = int(visible)
+            else:
+                idx = self.dev
+            if lib.nvmlDeviceGetHandleByIndex_v2(idx, C.byref(h)) != 0:
+                return False
+        self.nvml, self.handle = lib, h
+        return True
+
+    def _nvml_loop(self):
+        import ctypes as C
+        lib, h = self.nvml, self.handle
+        get_reasons = getattr(lib, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+            getattr(lib, "nvmlDeviceGetCurrentClocksThrottleReasons")
+        mx = C.c_uint(0)
+        lib.nvmlDeviceGetMaxClockInfo(h, self.NVML_CLOCK_SM, C.byref(mx))
+        while True:
+            mhz = C.c_uint(0)
+            why = C.c_ulonglong(0)
+            if lib.nvmlDeviceGetClockInfo(h, self.NVML_CLOCK_SM, C.byref(mhz)) == 0 and \
+                    get_reasons(h, C.byref(why)) == 0:
+                r = [name for name, bit in self.NVML_BITS.items() if why.value & bit]
+                self.rows.append((float(mhz.value), float(mx.value), r))
+            if self.stop.wait(0.005):
+                break
 
     def __enter__(self):
+        import threading
         try:
+            if self._nvml_handle():
+                self.source = "nvml, every 5 ms"
+                self.stop = threading.Event()
+                self.thread = threading.Thread(target=self._nvml_loop, daemon=True)
+                self.thread.start()
+                t0 = time.time()
+                while not self.rows and time.time() - t0 < 1.0:
+                    time.sleep(0.001)
+                return self
+        except Exception:
+            self.thread = None
+        try:
+            self.source = "nvidia-smi -lms 200"
             self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.dev), f"--query-gpu={self.FIELDS}",
                  "--format=csv,noheader,nounits", "-lms", "200"],
                 stdout=self.f, stderr=subprocess.DEVNULL)
+            t0 = time.time()
+            while time.time() - t0 < 3.0 and os.path.getsize(self.f.name) == 0:
+                time.sleep(0.01)
         except Exception:
             self.proc = None
         return self
 
     def __exit__(self, *a):
+        if self.thread:
+            self.stop.set()
+            self.thread.join(timeout=5)
         if self.proc:
             self.proc.terminate()
             try:
@@ -109,30 +188,41 @@ class Clocks:
             except Exception:
                 self.proc.kill()
 
-    def summary(self):
-        if not self.proc or not self.f:
-            return None
-        self.f.flush()
+    def _smi_rows(self):
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown",
+                 "sw_power_cap"]
         rows = []
+        self.f.flush()
         with open(self.f.name) as fh:
             for line in fh:
                 p = [x.strip() for x in line.split(",")]
                 if len(p) < 8:
                     continue
                 try:
-                    rows.append((float(p[0]), float(p[1]), p[4:8]))
+                    rows.append((float(p[0]), float(p[1]),
+                                 [names[k] for k in range(4)
+                                  if p[4 + k].lower().startswith("active")]))
                 except ValueError:
                     continue
         os.unlink(self.f.name)
+        return rows
+
+    def summary(self):
+        if self.thread:
+            rows = self.rows
+        elif self.proc and self.f:
+            rows = self._smi_rows()
+        else:
+            rows = []
+            if self.f:
+                os.unlink(self.f.name)
+                self.f = None
         if not rows:
             return None
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown",
-                 "sw_power_cap"]
-        reasons = sorted({names[k] for _, _, r in rows for k in range(4)
-                          if r[k].lower().startswith("active")})
+        reasons = sorted({x for _, _, r in rows for x in r})
         return {"sm_mhz": statistics.median(r[0] for r in rows),
                 "sm_max_mhz": max(r[1] for r in rows),
-                "reasons": reasons, "samples": len(rows)}
+                "reasons": reasons, "samples": len(rows), "source": self.source}
 
 
 def measured_peaks():
@@ -747,11 +837,11 @@ def main():
                 "traffic": TRAVERSE_DRAM_BYTES if n == 1_000_000 else None,
                 "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, "
                                   "one launch (profiles/kernels_sbm1m_full.md)",
-                "kernel": {"warp": "k_traverse_warp<float>",
-                           "thread": "k_traverse<float, 6>",
-                           "wide": "k_traverse<float, 1>",
-                           "pair": "k_traverse_multi<float, 2>",
-                           "quad": "k_traverse_multi<float, 4>"}[args.walk],
+                "kernel": {"warp": "k_traverse_warp<float, 0>",
+                           "thread": "k_traverse<float, 0, 6>",
+                           "wide": "k_traverse<float, 0, 1>",
+                           "pair": "k_traverse_multi<float, 0, 2>",
+                           "quad": "k_traverse_multi<float, 0, 4>"}[args.walk],
                 "peak_kind": f"{kind} (HBM copy)",
                 "launch_ms": ph["repulsion"],
                 "l2_request_bytes": l2_bytes,
