@@ -67,6 +67,31 @@ template <class R> struct Layout : LayoutBase {
     int n = 0, ninc = 0, repulsion = 0, adjust = 0, strong = 0, linlog = 0;
     int any_fixed = 0;
     int walk = WALK_THREAD;
+    int climb_mode = 1; // leaves per aggregate thread (negative: interleaved)
+
+    // Leaves per thread of the tree's climb, from the ratio x of leaves to
+    // the threads the device holds at once. Measured on a GB300 (FP32, SBM
+    // graphs, climb time in ms for 1 / 2 / 4 / 8 leaves per thread): 2e5
+    // leaves (x 0.64) 0.068 / 0.069 / 0.082 / 0.122; 4e5 (x 1.3) 0.099 /
+    // 0.083 / 0.096 / 0.139; 6e5 (x 1.9) 0.125 / 0.117 / 0.110 / 0.149; 1e6
+    // (x 3.2) 0.183 / 0.160 / 0.149 / 0.186; 2e6 (x 6.4) 0.318 / 0.253 /
+    // 0.265 / 0.322; 3e6 (x 9.6) 0.453 / 0.349 / 0.372 / 0.531. FP64 (fewer
+    // threads per SM): 4 leaves per thread was fastest or tied at 1e5 and
+    // 1e6 leaves (1e6: 0.554 / 0.382 / 0.334).
+    static int pick_climb(int n, int device)
+    {
+        if (sizeof(R) == 8) return n >= 50000 ? 4 : 1;
+        int sms = 0, blocks = 0;
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, k_aggregate<R>, 256, 0) !=
+                cudaSuccess ||
+            blocks < 1 || sms < 1) {
+            cudaGetLastError();
+            return 1;
+        }
+        const double x = (double) n / ((double) sms * blocks * 256.0);
+        return x < 1.0 ? 1 : x < 1.6 ? 2 : x < 5.0 ? 4 : 2;
+    }
     R scaling = 0, gravity = 0, theta2 = 0;
     double theta2d = 0.0;
     cudaStream_t s = nullptr;
@@ -248,6 +273,7 @@ template <class R> struct Layout : LayoutBase {
         mem.pool = opts ? opts->pool : nullptr;
         mem.s = s;
         if (rep == FA2CU_REPULSION_BH && sort_setup()) return 1;
+        if (rep == FA2CU_REPULSION_BH) climb_mode = pick_climb(n, device);
         if (rep == FA2CU_REPULSION_EXACT) {
             int sms = 0;
             cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
@@ -351,8 +377,31 @@ template <class R> struct Layout : LayoutBase {
         k_gather_karras<R><<<ceil_div(n, 256), 256, 0, s>>>(n, adjust, order, pos, mass, size,
                                                             psort, key, child, range, parent,
                                                             rope, visits, status);
-        k_aggregate<R><<<ceil_div(n, 256), 256, 0, s>>>(n, psort, child, parent, range, rope,
-                                                        visits, agg, nodes, status);
+        switch (climb_mode) {
+        case 2:
+            k_aggregate_multi<R, 2, true><<<ceil_div(n, 512), 256, 0, s>>>(
+                n, psort, child, parent, range, rope, visits, agg, nodes, status);
+            break;
+        case 4:
+            k_aggregate_multi<R, 4, true><<<ceil_div(n, 1024), 256, 0, s>>>(
+                n, psort, child, parent, range, rope, visits, agg, nodes, status);
+            break;
+        case 8:
+            k_aggregate_multi<R, 8, true><<<ceil_div(n, 2048), 256, 0, s>>>(
+                n, psort, child, parent, range, rope, visits, agg, nodes, status);
+            break;
+        case -2:
+            k_aggregate_multi<R, 2, false><<<ceil_div(n, 512), 256, 0, s>>>(
+                n, psort, child, parent, range, rope, visits, agg, nodes, status);
+            break;
+        case -4:
+            k_aggregate_multi<R, 4, false><<<ceil_div(n, 1024), 256, 0, s>>>(
+                n, psort, child, parent, range, rope, visits, agg, nodes, status);
+            break;
+        default:
+            k_aggregate<R><<<ceil_div(n, 256), 256, 0, s>>>(n, psort, child, parent, range,
+                                                            rope, visits, agg, nodes, status);
+        }
     }
     void launch_repulsion()
     {
@@ -630,6 +679,12 @@ template <class R> struct Layout : LayoutBase {
     {
         if (!strcmp(name, "sort_threads") && (value == 256 || value == 512 || value == 1024)) {
             ss.tile_threads = (int) value;
+            return recapture();
+        }
+        if (!strcmp(name, "climb") &&
+            (value == 1 || value == 2 || value == 4 || value == 8 || value == -2 ||
+             value == -4)) {
+            climb_mode = (int) value;
             return recapture();
         }
         if (!strcmp(name, "walk") &&

@@ -350,3 +350,27 @@ def test_warp_walk_equals_thread_walk(gpu, prec, adjust):
         np.testing.assert_array_equal(fw, ft)
     else:
         assert rel_err(fw, ft) <= 1e-6
+
+
+@pytest.mark.parametrize("prec", ["single", "double"])
+def test_climb_leaves_per_thread_give_the_same_tree(gpu, prec):
+    """The tree's sums are the same whichever thread completes a region: 1,
+    2, 4 or 8 leaves per climbing thread (contiguous or interleaved over the
+    warp) give the same regions, hence bit-identical forces and
+    trajectories, on a graph with coincident nodes."""
+    n, a, b = G.barabasi_albert(30000, 3, seed=6)
+    w = np.ones(len(a))
+    pos = f32(G.uniform_positions(n, -2000, 2000, seed=7))
+    pos[:64] = pos[np.tile(np.arange(8), 8)]
+    want_f = None
+    for mode in (1, 2, 4, 8, -2, -4):
+        with make_layout(n, a, b, w, pos, prec, theta=1.2) as L:
+            L.option("climb", mode)
+            f = L.forces(pos)
+            L.iterate(5)
+            L.sync()
+            xy = L.positions()
+        if want_f is None:
+            want_f, want_xy = f, xy
+        np.testing.assert_array_equal(f, want_f, err_msg=f"climb {mode}")
+        np.testing.assert_array_equal(xy, want_xy, err_msg=f"climb {mode}")
