@@ -265,22 +265,34 @@ k_morton(int n, const typename RT<R>::R2 *__restrict__ pos, const double *__rest
 {
     __shared__ SortHistShared H;
     if (aux) hist_begin(H, lookback, nlookback); // (uniform)
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const double minx = quant[0], miny = quant[1], scale = quant[2];
-        const typename RT<R>::R2 p = pos[i];
-        uint32_t cx, cy;
-        if constexpr (sizeof(R) == 4) {
-            const float4 qf = *reinterpret_cast<const float4 *>(quant + 4);
-            cx = morton_cell(p.x, qf.z, minx, scale, qf.x, qf.y);
-            cy = morton_cell(p.y, qf.w, miny, scale, qf.x, qf.y);
-        } else {
-            cx = morton_cell(p.x, minx, scale);
-            cy = morton_cell(p.y, miny, scale);
+    const double minx = quant[0], miny = quant[1], scale = quant[2];
+    float4 qf = make_float4(0.f, 0.f, 0.f, 0.f);
+    if constexpr (sizeof(R) == 4) qf = *reinterpret_cast<const float4 *>(quant + 4);
+    // U positions per thread loaded together, then coded
+    constexpr int U = 4;
+    const int stride = gridDim.x * blockDim.x;
+    for (int i0 = blockIdx.x * blockDim.x + threadIdx.x; i0 < n; i0 += U * stride) {
+        typename RT<R>::R2 p[U];
+#pragma unroll
+        for (int u = 0; u < U; u++)
+            if (i0 + u * stride < n) p[u] = pos[i0 + u * stride];
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            const int i = i0 + u * stride;
+            if (i >= n) break;
+            uint32_t cx, cy;
+            if constexpr (sizeof(R) == 4) {
+                cx = morton_cell(p[u].x, qf.z, minx, scale, qf.x, qf.y);
+                cy = morton_cell(p[u].y, qf.w, miny, scale, qf.x, qf.y);
+            } else {
+                cx = morton_cell(p[u].x, minx, scale);
+                cy = morton_cell(p[u].y, miny, scale);
+            }
+            const uint32_t k = spread16(cx) | (spread16(cy) << 1);
+            key[i] = k;
+            idx[i] = (uint32_t) i;
+            if (aux) hist_add(H, k, 4);
         }
-        const uint32_t k = spread16(cx) | (spread16(cy) << 1);
-        key[i] = k;
-        idx[i] = (uint32_t) i;
-        if (aux) hist_add(H, k, 4);
     }
     if (aux) hist_end(H, 4, aux);
 }
@@ -300,15 +312,20 @@ k_gather_karras(int n, int adjust, const uint32_t *__restrict__ order,
 {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
-    if (k < n - 1) karras_one<true>(k, n, key, child, range, parent, rope, visits);
+    // the node's record is loaded first, so that its scattered loads are in
+    // flight during the tree search
     const uint32_t i = order[k];
-    if (i >= (uint32_t) n) { // never for a valid sort
-        atomicOr(status + ST_ERROR, ERR_BOUNDS);
-        psort[k] = mk4<R>(R(0), R(0), R(0), R(0));
-        return;
+    const bool ok = i < (uint32_t) n; // always, for a valid sort
+    typename RT<R>::R2 p = mk2<R>(R(0), R(0));
+    R m = R(0), sz = R(0);
+    if (ok) {
+        p = pos[i];
+        m = mass[i];
+        if (adjust) sz = size[i];
     }
-    const typename RT<R>::R2 p = pos[i];
-    psort[k] = mk4<R>(p.x, p.y, mass[i], adjust ? size[i] : R(0));
+    if (k < n - 1) karras_one<true>(k, n, key, child, range, parent, rope, visits);
+    if (!ok) atomicOr(status + ST_ERROR, ERR_BOUNDS);
+    psort[k] = mk4<R>(p.x, p.y, m, sz);
 }
 
 // ---- 4c. bottom-up centres of mass (pipeline.cl:272-323) -------------------
