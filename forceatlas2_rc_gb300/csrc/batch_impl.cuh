@@ -414,9 +414,15 @@ k_batch(int ngraphs, BatchGraph *graphs, const int *queue, int *next, int iterat
                     karras_one<false>(i, n, key, child, range, parent, rope, visits);
                 __syncthreads();
                 phase(BP_TREE);
-                for (int k = tid; k < n; k += T)
-                    climb<R, true>(k, n, psort, child, parent, range, rope, visits, agg, nodes,
-                                   status);
+                // contiguous leaves per thread: a thread's later climbs find
+                // the regions of its earlier ones complete
+                const int per = (n + T - 1) / T;
+                for (int q = 0; q < per; q++) {
+                    const int k = tid * per + q;
+                    if (k < n)
+                        climb<R, true>(k, n, psort, child, parent, range, rope, visits, agg,
+                                       nodes, status);
+                }
                 __syncthreads();
                 phase(BP_SUMS);
                 for (int k = tid; k < n; k += T) {
