@@ -195,7 +195,8 @@ int fa2_gpu_device_info(int idx, fa2_gpu_devinfo *info)
         return 1;
     }
     memset(info, 0, sizeof(*info));
-    snprintf(info->name, sizeof(info->name), "%s", p.name);
+    // the device name is cut to the interface's 128 bytes
+    snprintf(info->name, sizeof(info->name), "%.*s", (int) sizeof(info->name) - 1, p.name);
     snprintf(info->vendor, sizeof(info->vendor), "NVIDIA Corporation");
     snprintf(info->platform, sizeof(info->platform), "CUDA");
     int rt = 0;
