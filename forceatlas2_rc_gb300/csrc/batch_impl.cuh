@@ -64,7 +64,8 @@ template <class R> struct BatchArrays {
     int2 *child, *range;
     int *parent, *rope, *visits;
     Agg<R> *agg;
-    BHNode<R> *nodes;
+    R4 *rec_c;  // traversal records (common.cuh)
+    int2 *rec_t;
     // per block, the cycles spent in each of the 8 phases of an iteration
     // (measurement launches only; nullptr otherwise)
     unsigned long long *prof;
@@ -240,7 +241,8 @@ k_batch(int ngraphs, BatchGraph *graphs, const int *queue, int *next, int iterat
         int2 *child = A.child + b0, *range = A.range + b0;
         int *parent = A.parent + 2 * (size_t) b0, *rope = A.rope + b0, *visits = A.visits + b0;
         Agg<R> *agg = A.agg + b0;
-        BHNode<R> *nodes = A.nodes + b0;
+        R4 *rec_c = A.rec_c + b0;
+        int2 *rec_t = A.rec_t + b0;
         if (tid == 0) {
             sh_speed = G->speed;
             sh_stop = 0;
@@ -421,16 +423,16 @@ k_batch(int ngraphs, BatchGraph *graphs, const int *queue, int *next, int iterat
                     const int k = tid * per + q;
                     if (k < n)
                         climb<R, true>(k, n, psort, child, parent, range, rope, visits, agg,
-                                       nodes, status);
+                                       rec_c, rec_t, status);
                 }
                 __syncthreads();
                 phase(BP_SUMS);
                 for (int k = tid; k < n; k += T) {
                     const R2 fk =
-                        adjust ? walk<R, true>(k, n, scaling, theta2, theta2d, psort, nodes,
-                                               agg, rope, status)
-                               : walk<R, false>(k, n, scaling, theta2, theta2d, psort, nodes,
-                                                agg, rope, status);
+                        adjust ? walk<R, true>(k, n, scaling, theta2, theta2d, psort, rec_c,
+                                               rec_t, agg, rope, status)
+                               : walk<R, false>(k, n, scaling, theta2, theta2d, psort, rec_c,
+                                                rec_t, agg, rope, status);
                     f[idx[k]] = fk;
                 }
             }
@@ -604,7 +606,8 @@ template <class R> struct Batch : BatchBase {
         A.rope = mem.get<int>(n1);
         A.visits = mem.get<int>(n1);
         A.agg = mem.get<Agg<R>>(n1);
-        A.nodes = mem.get<BHNode<R>>(n1);
+        A.rec_c = mem.get<R4>(n1);
+        A.rec_t = mem.get<int2>(n1);
         graphs = mem.get<BatchGraph>((size_t) G);
         queue = mem.get<int>((size_t) G);
         next = mem.get<int>(1);

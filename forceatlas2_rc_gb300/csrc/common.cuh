@@ -92,14 +92,22 @@ template <> struct RT<double> {
     typedef double4_32a R4;
 };
 
-// Tree-node record of the Barnes-Hut traversal: centre of mass, mass and
-// squared size, then the left child, the next node that is not a descendant
-// (-1 at the end) and the range of sorted nodes covered. 32 bytes in float,
-// 64 in double; one record per internal node of the Karras tree.
-template <class R> struct alignas(sizeof(R) * 4 >= 32 ? 64 : 32) BHNode {
-    typename RT<R>::R4 c;  // cx, cy, m, size^2
-    int4 t;                // left, skip, first, last
-};
+// Traversal records of the n-1 regions of the Karras tree, in two arrays
+// (a walk step reads 16 + 8 bytes in float, 32 + 8 in double):
+//   rec_c[r] = (cx, cy, m, size^2);
+//   rec_t[r] = (left, skip): the left child, and the next region that is not
+//   a descendant (-1 at the end). A region of at most 8 nodes is never
+//   opened; its left link carries its range of sorted nodes instead,
+//   ~(first | (last - first) << 27), negative (first < 2^27).
+__host__ __device__ __forceinline__ int bucket_pack(int first, int last)
+{
+    return ~(first | ((last - first) << 27));
+}
+__host__ __device__ __forceinline__ int bucket_first(int left) { return ~left & ((1 << 27) - 1); }
+__host__ __device__ __forceinline__ int bucket_last(int left)
+{
+    return (~left & ((1 << 27) - 1)) + (~left >> 27);
+}
 
 // One CSR incidence: the node at the other end and the attraction strength.
 template <class R> struct alignas(2 * sizeof(R) > 8 ? 16 : 8) Inc {

@@ -484,14 +484,14 @@ template <bool CTA> __device__ __forceinline__ int arrive(int *v)
 }
 
 // The climb of leaf k (sorted position) of an n-node tree: every region it
-// reaches second gets its sums (agg) and its traversal record (nodes).
+// reaches second gets its sums (agg) and its traversal records.
 template <class R, bool CTA>
 __device__ __forceinline__ void climb(int k, int n, const typename RT<R>::R4 *psort,
                                       const int2 *child,
                                       const int *parent,
                                       const int2 *range,
                                       const int *rope, int *visits,
-                                      Agg<R> *agg, BHNode<R> *nodes,
+                                      Agg<R> *agg, typename RT<R>::R4 *rec_c, int2 *rec_t,
                                       int *status)
 {
     const int nl = n - 1;
@@ -513,12 +513,10 @@ __device__ __forceinline__ void climb(int k, int n, const typename RT<R>::R4 *ps
         const Agg<R> q = agg_combine(a, b);
         agg[r] = q;
         const int2 rg = range[r];
-        BHNode<R> nd;
-        nd.c = agg_record(q);
+        rec_c[r] = agg_record(q);
         // a region of at most 8 nodes is never opened: its left link
-        // carries ~first instead, so that the walk tells it by the sign
-        nd.t = make_int4(rg.y - rg.x >= 8 ? c.x : ~rg.x, rope[rg.y], rg.x, rg.y);
-        nodes[r] = nd;
+        // carries its packed range instead (negative)
+        rec_t[r] = make_int2(rg.y - rg.x >= 8 ? c.x : bucket_pack(rg.x, rg.y), rope[rg.y]);
         r = parent[r];
     }
 }
@@ -529,10 +527,13 @@ k_aggregate(int n, const typename RT<R>::R4 *__restrict__ psort,
             const int2 *__restrict__ child, const int *__restrict__ parent,
             const int2 *__restrict__ range, const int *__restrict__ rope,
             int *__restrict__ visits, Agg<R> *__restrict__ agg,
-            BHNode<R> *__restrict__ nodes, int *__restrict__ status)
+            typename RT<R>::R4 *__restrict__ rec_c, int2 *__restrict__ rec_t,
+            int *__restrict__ status)
 {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k < n) climb<R, false>(k, n, psort, child, parent, range, rope, visits, agg, nodes, status);
+    if (k < n)
+        climb<R, false>(k, n, psort, child, parent, range, rope, visits, agg, rec_c, rec_t,
+                        status);
 }
 
 // The climbs of P leaves per thread, one after the other: with n/P threads
@@ -541,19 +542,23 @@ k_aggregate(int n, const typename RT<R>::R4 *__restrict__ psort,
 // wave to finish the region above it. CONTIG: thread t takes leaves tP ..
 // tP+P-1; else lane l of warp w takes leaves (wP+q)32+l, q < P. Which thread
 // computes a region does not change what it computes: the tree is the same.
+// In float the launch bound keeps 2048 threads per SM (32 registers), which
+// the choice of P (pick_climb) counts on.
 template <class R, int P, bool CONTIG>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, sizeof(R) == 4 ? 8 : 4)
 k_aggregate_multi(int n, const typename RT<R>::R4 *__restrict__ psort,
                   const int2 *__restrict__ child, const int *__restrict__ parent,
                   const int2 *__restrict__ range, const int *__restrict__ rope,
                   int *__restrict__ visits, Agg<R> *__restrict__ agg,
-                  BHNode<R> *__restrict__ nodes, int *__restrict__ status)
+                  typename RT<R>::R4 *__restrict__ rec_c, int2 *__restrict__ rec_t,
+            int *__restrict__ status)
 {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     for (int q = 0; q < P; q++) {
         const int k = CONTIG ? t * P + q : ((t >> 5) * P + q) * 32 + (t & 31);
         if (k < n)
-            climb<R, false>(k, n, psort, child, parent, range, rope, visits, agg, nodes, status);
+            climb<R, false>(k, n, psort, child, parent, range, rope, visits, agg, rec_c, rec_t,
+                            status);
     }
 }
 
@@ -601,7 +606,7 @@ __device__ __forceinline__ bool far_dd(const Agg<double> *a, float xi, float yi,
 template <class R, bool ADJUST>
 __device__ __forceinline__ typename RT<R>::R2
 walk(int k, int n, R scaling, R theta2, double theta2d,
-     const typename RT<R>::R4 *psort, const BHNode<R> *nodes,
+     const typename RT<R>::R4 *psort, const typename RT<R>::R4 *rec_c, const int2 *rec_t,
      const Agg<R> *agg, const int *rope, int *status)
 {
     typedef typename RT<R>::R4 R4;
@@ -638,28 +643,29 @@ walk(int k, int n, R scaling, R theta2, double theta2d,
             cur = rope[j];
             continue;
         }
-        const BHNode<R> nd = nodes[cur];
-        const R xd = xi - nd.c.x, yd = yi - nd.c.y;
+        const R4 c = rec_c[cur];
+        const int2 t = rec_t[cur];
+        const R xd = xi - c.x, yd = yi - c.y;
         const R d2 = xd * xd + yd * yd;
         const R lhs = d2 * theta2;
-        bool far = lhs > nd.c.w;
-        if (sizeof(R) == 4 && fabs_r(lhs - nd.c.w) <= R(DECIDE_BAND) * nd.c.w)
+        bool far = lhs > c.w;
+        if (sizeof(R) == 4 && fabs_r(lhs - c.w) <= R(DECIDE_BAND) * c.w)
             far = far_dd(agg + cur, (float) xi, (float) yi, theta2d);
         if (far) {
-            const R g = fdiv(scaling * (mi * nd.c.z), d2);
+            const R g = fdiv(scaling * (mi * c.z), d2);
             ax += xd * g;
             ay += yd * g;
-            cur = nd.t.y;
-        } else if (nd.t.x >= 0) {
-            cur = nd.t.x;
+            cur = t.y;
+        } else if (t.x >= 0) {
+            cur = t.x;
         } else { // at most 8 nodes: node by node
-            j = nd.t.z;
-            jend = nd.t.w;
-            if (j < 0 || jend >= n) {
+            j = bucket_first(t.x);
+            jend = bucket_last(t.x);
+            if (jend >= n) {
                 atomicOr(status + ST_ERROR, ERR_BOUNDS);
                 break;
             }
-            cur = nd.t.y;
+            cur = t.y;
         }
     }
     return mk2<R>(ax, ay);
@@ -669,14 +675,15 @@ template <class R, bool ADJUST, int MINB>
 __global__ void __launch_bounds__(256, MINB)
 k_traverse(int n, R scaling, R theta2, double theta2d,
            const typename RT<R>::R4 *__restrict__ psort,
-           const BHNode<R> *__restrict__ nodes, const Agg<R> *__restrict__ agg,
-           const int *__restrict__ rope, const uint32_t *__restrict__ order,
-           typename RT<R>::R2 *__restrict__ f, int *__restrict__ status)
+           const typename RT<R>::R4 *__restrict__ rec_c, const int2 *__restrict__ rec_t,
+           const Agg<R> *__restrict__ agg, const int *__restrict__ rope,
+           const uint32_t *__restrict__ order, typename RT<R>::R2 *__restrict__ f,
+           int *__restrict__ status)
 {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
-    f[order[k]] = walk<R, ADJUST>(k, n, scaling, theta2, theta2d, psort, nodes, agg, rope,
-                                  status);
+    f[order[k]] = walk<R, ADJUST>(k, n, scaling, theta2, theta2d, psort, rec_c, rec_t, agg,
+                                  rope, status);
 }
 
 // The walk of P sorted nodes k0 .. k0+cnt-1 (cnt <= P, neighbours in
@@ -691,8 +698,9 @@ k_traverse(int n, R scaling, R theta2, double theta2d,
 template <class R, bool ADJUST, int P>
 __device__ __forceinline__ void
 walk_multi(int k0, int cnt, int n, R scaling, R theta2, double theta2d,
-           const typename RT<R>::R4 *psort, const BHNode<R> *nodes, const Agg<R> *agg,
-           const int *rope, const uint32_t *order, typename RT<R>::R2 *f, int *status)
+           const typename RT<R>::R4 *psort, const typename RT<R>::R4 *rec_c,
+           const int2 *rec_t, const Agg<R> *agg, const int *rope, const uint32_t *order,
+           typename RT<R>::R2 *f, int *status)
 {
     typedef typename RT<R>::R4 R4;
     constexpr int ACTIVE = -2;
@@ -745,35 +753,36 @@ walk_multi(int k0, int cnt, int n, R scaling, R theta2, double theta2d,
             cur = rope[j];
             continue;
         }
-        const BHNode<R> nd = nodes[cur];
+        const R4 c = rec_c[cur];
+        const int2 t = rec_t[cur];
         unsigned nearm = 0;
 #pragma unroll
         for (int u = 0; u < P; u++) {
             if (!((act >> u) & 1u)) continue;
-            const R xd = xi[u] - nd.c.x, yd = yi[u] - nd.c.y;
+            const R xd = xi[u] - c.x, yd = yi[u] - c.y;
             const R d2 = xd * xd + yd * yd;
             const R lhs = d2 * theta2;
-            bool far = lhs > nd.c.w;
-            if (sizeof(R) == 4 && fabs_r(lhs - nd.c.w) <= R(DECIDE_BAND) * nd.c.w)
+            bool far = lhs > c.w;
+            if (sizeof(R) == 4 && fabs_r(lhs - c.w) <= R(DECIDE_BAND) * c.w)
                 far = far_dd(agg + cur, (float) xi[u], (float) yi[u], theta2d);
             if (far) {
-                const R g = fdiv(scaling * (mi[u] * nd.c.z), d2);
+                const R g = fdiv(scaling * (mi[u] * c.z), d2);
                 ax[u] += xd * g;
                 ay[u] += yd * g;
-                resume[u] = nd.t.y;
+                resume[u] = t.y;
             } else {
                 nearm |= 1u << u;
             }
         }
         if (nearm == 0) {
-            cur = nd.t.y;
-        } else if (nd.t.x >= 0) {
-            cur = nd.t.x;
+            cur = t.y;
+        } else if (t.x >= 0) {
+            cur = t.x;
         } else {
-            j = nd.t.z;
-            jend = nd.t.w;
+            j = bucket_first(t.x);
+            jend = bucket_last(t.x);
             pairs = nearm;
-            cur = nd.t.y;
+            cur = t.y;
         }
     }
 #pragma unroll
@@ -785,14 +794,15 @@ template <class R, bool ADJUST, int P>
 __global__ void __launch_bounds__(256)
 k_traverse_multi(int n, R scaling, R theta2, double theta2d,
                  const typename RT<R>::R4 *__restrict__ psort,
-                 const BHNode<R> *__restrict__ nodes, const Agg<R> *__restrict__ agg,
+                 const typename RT<R>::R4 *__restrict__ rec_c,
+                 const int2 *__restrict__ rec_t, const Agg<R> *__restrict__ agg,
                  const int *__restrict__ rope, const uint32_t *__restrict__ order,
                  typename RT<R>::R2 *__restrict__ f, int *__restrict__ status)
 {
     const int k0 = (blockIdx.x * blockDim.x + threadIdx.x) * P;
     if (k0 >= n) return;
-    walk_multi<R, ADJUST, P>(k0, min(P, n - k0), n, scaling, theta2, theta2d, psort, nodes,
-                             agg, rope, order, f, status);
+    walk_multi<R, ADJUST, P>(k0, min(P, n - k0), n, scaling, theta2, theta2d, psort, rec_c,
+                             rec_t, agg, rope, order, f, status);
 }
 
 // The same walk, warp-synchronous. The 32 threads of a warp (neighbours in
@@ -808,9 +818,11 @@ template <class R, bool ADJUST>
 __global__ void __launch_bounds__(256)
 k_traverse_warp(int n, R scaling, R theta2, double theta2d,
                 const typename RT<R>::R4 *__restrict__ psort,
-                const BHNode<R> *__restrict__ nodes, const Agg<R> *__restrict__ agg,
-                const int *__restrict__ rope, const uint32_t *__restrict__ order,
-                typename RT<R>::R2 *__restrict__ f, int *__restrict__ status)
+                const typename RT<R>::R4 *__restrict__ rec_c,
+                const int2 *__restrict__ rec_t, const int2 *__restrict__ range,
+                const Agg<R> *__restrict__ agg, const int *__restrict__ rope,
+                const uint32_t *__restrict__ order, typename RT<R>::R2 *__restrict__ f,
+                int *__restrict__ status)
 {
     typedef typename RT<R>::R4 R4;
     const unsigned FULL = 0xffffffffu;
@@ -843,29 +855,31 @@ k_traverse_warp(int n, R scaling, R theta2, double theta2d,
             cur = rope[j];
             continue;
         }
-        const BHNode<R> nd = nodes[cur];
+        const R4 c = rec_c[cur];
+        const int2 t = rec_t[cur];
+        const int2 rg = range[cur]; // first, last
         bool open = false, direct = false;
-        if (nd.t.z >= resume) {
-            const R xd = xi - nd.c.x, yd = yi - nd.c.y;
+        if (rg.x >= resume) {
+            const R xd = xi - c.x, yd = yi - c.y;
             const R d2 = xd * xd + yd * yd;
             const R lhs = d2 * theta2;
-            bool far = lhs > nd.c.w;
-            if (sizeof(R) == 4 && fabs_r(lhs - nd.c.w) <= R(DECIDE_BAND) * nd.c.w)
+            bool far = lhs > c.w;
+            if (sizeof(R) == 4 && fabs_r(lhs - c.w) <= R(DECIDE_BAND) * c.w)
                 far = far_dd(agg + cur, (float) xi, (float) yi, theta2d);
             if (far) {
-                const R g = fdiv(scaling * (mi * nd.c.z), d2);
+                const R g = fdiv(scaling * (mi * c.z), d2);
                 ax += xd * g;
                 ay += yd * g;
-                resume = nd.t.w + 1;
-            } else if (nd.t.x >= 0) {
+                resume = rg.y + 1;
+            } else if (t.x >= 0) {
                 open = true;
             } else {
                 direct = true;
-                resume = nd.t.w + 1;
+                resume = rg.y + 1;
             }
         }
         if (__any_sync(FULL, direct)) {
-            for (int j = nd.t.z; j <= nd.t.w; j++) {
+            for (int j = rg.x; j <= rg.y; j++) {
                 const R4 q = psort[j];
                 if (direct && j != k) {
                     const R xd = xi - q.x, yd = yi - q.y;
@@ -876,7 +890,7 @@ k_traverse_warp(int n, R scaling, R theta2, double theta2d,
                 }
             }
         }
-        cur = __any_sync(FULL, open) ? nd.t.x : nd.t.y;
+        cur = __any_sync(FULL, open) ? t.x : t.y;
     }
     if (valid) f[order[k]] = mk2<R>(ax, ay);
 }
@@ -886,7 +900,8 @@ k_traverse_warp(int n, R scaling, R theta2, double theta2d,
 template <class R>
 __global__ void __launch_bounds__(256)
 k_traverse_count(int n, R theta2, double theta2d, const typename RT<R>::R4 *__restrict__ psort,
-                 const BHNode<R> *__restrict__ nodes, const Agg<R> *__restrict__ agg,
+                 const typename RT<R>::R4 *__restrict__ rec_c,
+                 const int2 *__restrict__ rec_t, const Agg<R> *__restrict__ agg,
                  const int *__restrict__ rope, unsigned long long *__restrict__ counts)
 {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -902,20 +917,22 @@ k_traverse_count(int n, R theta2, double theta2d, const typename RT<R>::R4 *__re
                 continue;
             }
             ++visits;
-            const BHNode<R> nd = nodes[cur];
-            const R xd = me.x - nd.c.x, yd = me.y - nd.c.y;
+            const typename RT<R>::R4 c = rec_c[cur];
+            const int2 t = rec_t[cur];
+            const R xd = me.x - c.x, yd = me.y - c.y;
             const R d2 = xd * xd + yd * yd;
             const R lhs = d2 * theta2;
-            bool far = lhs > nd.c.w;
-            if (sizeof(R) == 4 && fabs_r(lhs - nd.c.w) <= R(DECIDE_BAND) * nd.c.w)
+            bool far = lhs > c.w;
+            if (sizeof(R) == 4 && fabs_r(lhs - c.w) <= R(DECIDE_BAND) * c.w)
                 far = far_dd(agg + cur, (float) me.x, (float) me.y, theta2d);
             if (far) {
-                cur = nd.t.y;
-            } else if (nd.t.x >= 0) {
-                cur = nd.t.x;
+                cur = t.y;
+            } else if (t.x >= 0) {
+                cur = t.x;
             } else {
-                pairs += nd.t.w - nd.t.z + 1 - (k >= nd.t.z && k <= nd.t.w);
-                cur = nd.t.y;
+                const int first = bucket_first(t.x), last = bucket_last(t.x);
+                pairs += last - first + 1 - (k >= first && k <= last);
+                cur = t.y;
             }
         }
     }

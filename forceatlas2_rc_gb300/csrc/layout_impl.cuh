@@ -11,7 +11,7 @@
 //   psort               R4[n]   (x, y, m, r) in Morton order
 //   child, range        int2[n-1], parent int[2n-1], rope int[n],
 //   visits              int[n-1], agg Agg<R>[n-1] (double / float-float sums),
-//                       nodes BHNode<R>[n-1]
+//                       rec_c R4[n-1], rec_t int2[n-1] (traversal records)
 //   bbox, quant         the bounding box and Morton quantisation, computed by
 //                       the displacement of the previous iteration
 //   packed, exact_part  R4[n], R2[rows n]  (exact repulsion only)
@@ -70,27 +70,28 @@ template <class R> struct Layout : LayoutBase {
     int climb_mode = 1; // leaves per aggregate thread (negative: interleaved)
 
     // Leaves per thread of the tree's climb, from the ratio x of leaves to
-    // the threads the device holds at once. Measured on a GB300 (FP32, SBM
-    // graphs, climb time in ms for 1 / 2 / 4 / 8 leaves per thread): 2e5
-    // leaves (x 0.64) 0.068 / 0.069 / 0.082 / 0.122; 4e5 (x 1.3) 0.099 /
-    // 0.083 / 0.096 / 0.139; 6e5 (x 1.9) 0.125 / 0.117 / 0.110 / 0.149; 1e6
-    // (x 3.2) 0.183 / 0.160 / 0.149 / 0.186; 2e6 (x 6.4) 0.318 / 0.253 /
-    // 0.265 / 0.322; 3e6 (x 9.6) 0.453 / 0.349 / 0.372 / 0.531. FP64 (fewer
-    // threads per SM): 4 leaves per thread was fastest or tied at 1e5 and
-    // 1e6 leaves (1e6: 0.554 / 0.382 / 0.334).
+    // the threads the device holds at once (2048 per SM in float). Measured
+    // on a GB300 (FP32, SBM graphs, climb time in ms for 1 / 2 / 4 / 8
+    // leaves per thread): 2e5 leaves (x 0.64) 0.069 / 0.074 / 0.084 / 0.123;
+    // 4e5 (x 1.3) 0.101 / 0.091 / 0.100 / 0.142; 6e5 (x 1.9) 0.128 / 0.107 /
+    // 0.117 / 0.155; 1e6 (x 3.2) 0.186 / 0.157 / 0.159 / 0.199; 2e6 (x 6.4)
+    // 0.326 / 0.263 / 0.289 / 0.387; 3e6 (x 9.6) 0.459 / 0.355 / 0.410 /
+    // 0.629. FP64 (fewer threads per SM): 4 leaves per thread was fastest or
+    // tied at 1e5 and 1e6 leaves (1e6: 0.554 / 0.382 / 0.334).
     static int pick_climb(int n, int device)
     {
         if (sizeof(R) == 8) return n >= 50000 ? 4 : 1;
         int sms = 0, blocks = 0;
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, k_aggregate<R>, 256, 0) !=
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, k_aggregate_multi<R, 2, true>,
+                                                          256, 0) !=
                 cudaSuccess ||
             blocks < 1 || sms < 1) {
             cudaGetLastError();
             return 1;
         }
         const double x = (double) n / ((double) sms * blocks * 256.0);
-        return x < 1.0 ? 1 : x < 1.6 ? 2 : x < 5.0 ? 4 : 2;
+        return x < 1.0 ? 1 : 2;
     }
     R scaling = 0, gravity = 0, theta2 = 0;
     double theta2d = 0.0;
@@ -112,7 +113,8 @@ template <class R> struct Layout : LayoutBase {
     int2 *child = nullptr, *range = nullptr;
     int *parent = nullptr, *rope = nullptr, *visits = nullptr;
     Agg<R> *agg = nullptr;
-    BHNode<R> *nodes = nullptr;
+    R4 *rec_c = nullptr; // traversal records (common.cuh)
+    int2 *rec_t = nullptr;
     double2 *swing_partial = nullptr;
     SpeedState *st = nullptr;
     int *status = nullptr;
@@ -172,7 +174,8 @@ template <class R> struct Layout : LayoutBase {
             rope = mem.get<int>(nn);
             visits = mem.get<int>(nn - 1);
             agg = mem.get<Agg<R>>(nn - 1);
-            nodes = mem.get<BHNode<R>>(nn - 1);
+            rec_c = mem.get<R4>(nn - 1);
+            rec_t = mem.get<int2>(nn - 1);
         } else {
             packed = mem.get<R4>(nn);
             if (exact_nrows > 1) exact_part = mem.get<R2>((size_t) exact_nrows * nn);
@@ -380,27 +383,28 @@ template <class R> struct Layout : LayoutBase {
         switch (climb_mode) {
         case 2:
             k_aggregate_multi<R, 2, true><<<ceil_div(n, 512), 256, 0, s>>>(
-                n, psort, child, parent, range, rope, visits, agg, nodes, status);
+                n, psort, child, parent, range, rope, visits, agg, rec_c, rec_t, status);
             break;
         case 4:
             k_aggregate_multi<R, 4, true><<<ceil_div(n, 1024), 256, 0, s>>>(
-                n, psort, child, parent, range, rope, visits, agg, nodes, status);
+                n, psort, child, parent, range, rope, visits, agg, rec_c, rec_t, status);
             break;
         case 8:
             k_aggregate_multi<R, 8, true><<<ceil_div(n, 2048), 256, 0, s>>>(
-                n, psort, child, parent, range, rope, visits, agg, nodes, status);
+                n, psort, child, parent, range, rope, visits, agg, rec_c, rec_t, status);
             break;
         case -2:
             k_aggregate_multi<R, 2, false><<<ceil_div(n, 512), 256, 0, s>>>(
-                n, psort, child, parent, range, rope, visits, agg, nodes, status);
+                n, psort, child, parent, range, rope, visits, agg, rec_c, rec_t, status);
             break;
         case -4:
             k_aggregate_multi<R, 4, false><<<ceil_div(n, 1024), 256, 0, s>>>(
-                n, psort, child, parent, range, rope, visits, agg, nodes, status);
+                n, psort, child, parent, range, rope, visits, agg, rec_c, rec_t, status);
             break;
         default:
             k_aggregate<R><<<ceil_div(n, 256), 256, 0, s>>>(n, psort, child, parent, range,
-                                                            rope, visits, agg, nodes, status);
+                                                            rope, visits, agg, rec_c, rec_t,
+                                                            status);
         }
     }
     void launch_repulsion()
@@ -409,40 +413,42 @@ template <class R> struct Layout : LayoutBase {
             if (walk == WALK_WARP) {
                 if (adjust)
                     k_traverse_warp<R, true><<<ceil_div(n, 256), 256, 0, s>>>(
-                        n, scaling, theta2, theta2d, psort, nodes, agg, rope, order, f, status);
+                        n, scaling, theta2, theta2d, psort, rec_c, rec_t, range, agg, rope, order, f,
+                        status);
                 else
                     k_traverse_warp<R, false><<<ceil_div(n, 256), 256, 0, s>>>(
-                        n, scaling, theta2, theta2d, psort, nodes, agg, rope, order, f, status);
+                        n, scaling, theta2, theta2d, psort, rec_c, rec_t, range, agg, rope, order, f,
+                        status);
             } else if (walk == WALK_THREAD) {
                 if (adjust)
                     k_traverse<R, true, 6><<<ceil_div(n, 256), 256, 0, s>>>(
-                        n, scaling, theta2, theta2d, psort, nodes, agg, rope, order, f, status);
+                        n, scaling, theta2, theta2d, psort, rec_c, rec_t, agg, rope, order, f, status);
                 else
                     k_traverse<R, false, 6><<<ceil_div(n, 256), 256, 0, s>>>(
-                        n, scaling, theta2, theta2d, psort, nodes, agg, rope, order, f, status);
+                        n, scaling, theta2, theta2d, psort, rec_c, rec_t, agg, rope, order, f, status);
             } else if (walk == WALK_PAIR) {
                 const int grid = ceil_div(ceil_div(n, 2), 256);
                 if (adjust)
                     k_traverse_multi<R, true, 2><<<grid, 256, 0, s>>>(
-                        n, scaling, theta2, theta2d, psort, nodes, agg, rope, order, f, status);
+                        n, scaling, theta2, theta2d, psort, rec_c, rec_t, agg, rope, order, f, status);
                 else
                     k_traverse_multi<R, false, 2><<<grid, 256, 0, s>>>(
-                        n, scaling, theta2, theta2d, psort, nodes, agg, rope, order, f, status);
+                        n, scaling, theta2, theta2d, psort, rec_c, rec_t, agg, rope, order, f, status);
             } else if (walk == WALK_QUAD) {
                 const int grid = ceil_div(ceil_div(n, 4), 256);
                 if (adjust)
                     k_traverse_multi<R, true, 4><<<grid, 256, 0, s>>>(
-                        n, scaling, theta2, theta2d, psort, nodes, agg, rope, order, f, status);
+                        n, scaling, theta2, theta2d, psort, rec_c, rec_t, agg, rope, order, f, status);
                 else
                     k_traverse_multi<R, false, 4><<<grid, 256, 0, s>>>(
-                        n, scaling, theta2, theta2d, psort, nodes, agg, rope, order, f, status);
+                        n, scaling, theta2, theta2d, psort, rec_c, rec_t, agg, rope, order, f, status);
             } else {
                 if (adjust)
                     k_traverse<R, true, 1><<<ceil_div(n, 256), 256, 0, s>>>(
-                        n, scaling, theta2, theta2d, psort, nodes, agg, rope, order, f, status);
+                        n, scaling, theta2, theta2d, psort, rec_c, rec_t, agg, rope, order, f, status);
                 else
                     k_traverse<R, false, 1><<<ceil_div(n, 256), 256, 0, s>>>(
-                        n, scaling, theta2, theta2d, psort, nodes, agg, rope, order, f, status);
+                        n, scaling, theta2, theta2d, psort, rec_c, rec_t, agg, rope, order, f, status);
             }
         } else {
             k_pack<R><<<ceil_div(n, 256), 256, 0, s>>>(n, adjust, pos, mass, size, packed);
@@ -644,20 +650,20 @@ template <class R> struct Layout : LayoutBase {
         launch_build();
         launch_sort();
         launch_tree();
-        std::vector<BHNode<R>> hn((size_t) n - 1);
+        std::vector<R4> hc((size_t) n - 1);
         const size_t nn = (size_t) n;
         cudaMemcpyAsync(hkey, key, nn * 4, cudaMemcpyDeviceToHost, s);
         cudaMemcpyAsync(horder, order, nn * 4, cudaMemcpyDeviceToHost, s);
         cudaMemcpyAsync(hchild, child, (nn - 1) * sizeof(int2), cudaMemcpyDeviceToHost, s);
         cudaMemcpyAsync(hrange, range, (nn - 1) * sizeof(int2), cudaMemcpyDeviceToHost, s);
         cudaMemcpyAsync(hparent, parent, (2 * nn - 1) * sizeof(int), cudaMemcpyDeviceToHost, s);
-        cudaMemcpyAsync(hn.data(), nodes, (nn - 1) * sizeof(BHNode<R>), cudaMemcpyDeviceToHost, s);
+        cudaMemcpyAsync(hc.data(), rec_c, (nn - 1) * sizeof(R4), cudaMemcpyDeviceToHost, s);
         FA2_TRY(cudaStreamSynchronize(s), "could not fetch the tree", 1);
         for (size_t r = 0; r + 1 < nn; r++) {
-            hni[4 * r] = (double) hn[r].c.x;
-            hni[4 * r + 1] = (double) hn[r].c.y;
-            hni[4 * r + 2] = (double) hn[r].c.z;
-            hni[4 * r + 3] = (double) hn[r].c.w;
+            hni[4 * r] = (double) hc[r].x;
+            hni[4 * r + 1] = (double) hc[r].y;
+            hni[4 * r + 2] = (double) hc[r].z;
+            hni[4 * r + 3] = (double) hc[r].w;
         }
         return 0;
     }
@@ -708,8 +714,8 @@ template <class R> struct Layout : LayoutBase {
         launch_sort();
         launch_tree();
         cudaMemsetAsync(counts, 0, 2 * sizeof(unsigned long long), s);
-        k_traverse_count<R><<<ceil_div(n, 256), 256, 0, s>>>(n, theta2, theta2d, psort, nodes,
-                                                             agg, rope, counts);
+        k_traverse_count<R><<<ceil_div(n, 256), 256, 0, s>>>(n, theta2, theta2d, psort, rec_c,
+                                                             rec_t, agg, rope, counts);
         unsigned long long h[2] = {0, 0};
         cudaMemcpyAsync(h, counts, sizeof(h), cudaMemcpyDeviceToHost, s);
         FA2_TRY(cudaStreamSynchronize(s), "the computation on the GPU failed", 1);
