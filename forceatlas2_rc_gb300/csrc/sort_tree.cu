@@ -112,57 +112,86 @@ k_sort_onesweep(int n, int pass, const uint32_t *__restrict__ kin,
         rk[r] = valid ? prior + lt : 0xffffffffu;
     }
     __syncthreads();
-    // per digit (threads 0..255): exclusive prefix over the warps, the
-    // tile's count, then the tile's offset inside the digit from the
-    // look-back
+    // per digit (threads 0..255): exclusive prefix over the warps and the
+    // tile's count, published at once
+    constexpr int W = T / 256; // lookers per digit
+    __shared__ uint32_t lb_part[W][256];
+    __shared__ int lb_stop[W][256]; // -2 all counts, -1 a prefix, else the unpublished tile
+    __shared__ int lb_next[256];    // next tile to read back from (-1: done)
+    __shared__ uint32_t lb_excl[256];
+    const int dg = threadIdx.x & 255, looker = threadIdx.x >> 8;
     uint32_t run = 0;
     if (threadIdx.x < 256) {
-        const int d = threadIdx.x;
 #pragma unroll 8
         for (int ww = 0; ww < NW; ww++) {
-            const uint32_t c = wh[ww][d];
-            wh[ww][d] = run;
+            const uint32_t c = wh[ww][dg];
+            wh[ww][dg] = run;
             run += c;
         }
-        uint32_t *me = status + (size_t) tile * 256 + d;
-        uint32_t excl = 0;
-        if (tile == 0) {
-            lb_store(me, LB_PREFIX | run);
-        } else {
-            lb_store(me, LB_COUNT | run);
-            const unsigned long long t0 = global_ns();
-            bool gave_up = false;
-            // windows of 16 predecessors, loaded together, used in order
-            // until a prefix (done) or a word not yet published (load again)
-            for (int j = tile - 1; j >= 0;) {
-                uint32_t x[16];
+        lb_store(status + (size_t) tile * 256 + dg, (tile == 0 ? LB_PREFIX : LB_COUNT) | run);
+        lb_next[dg] = tile - 1;
+        lb_excl[dg] = 0;
+    }
+    __syncthreads();
+    // the look-back: each round, looker w of a digit reads the 16 tiles
+    // from lb_next - 16w down (together W * 16 predecessors), summing counts
+    // until it meets a prefix (done) or a word not yet published; the
+    // digit's thread takes the windows in order, up to the first that did
+    // not hold counts only, and goes on from an unpublished tile. Bounded in
+    // time: after 1 s a digit gives up (error flag).
+    const unsigned long long t0 = global_ns();
+    bool gave_up = false;
+    for (;;) {
+        const int j0 = lb_next[dg];
+        if (j0 >= 0) {
+            const int jb = j0 - 16 * looker;
+            uint32_t x[16];
 #pragma unroll
-                for (int q = 0; q < 16; q++)
-                    x[q] = j - q >= 0 ? lb_load(status + (size_t) (j - q) * 256 + d) : LB_PREFIX;
-                bool done = false, stalled = false;
+            for (int q = 0; q < 16; q++)
+                x[q] = jb - q >= 0 ? lb_load(status + (size_t) (jb - q) * 256 + dg) : LB_PREFIX;
+            uint32_t sum = 0;
+            int stop = -2;
 #pragma unroll
-                for (int q = 0; q < 16; q++) {
-                    if (done || stalled) continue;
-                    if (x[q] & LB_PREFIX) {
-                        excl += x[q] & LB_MASK;
-                        done = true;
-                    } else if (x[q] & LB_COUNT) {
-                        excl += x[q] & LB_MASK;
-                        j--;
-                    } else {
-                        stalled = true;
-                    }
-                }
-                if (done) break;
-                if (stalled && global_ns() - t0 > 1000000000ull) {
-                    gave_up = true; // 1 s: a predecessor never published
+            for (int q = 0; q < 16; q++) {
+                if (stop != -2) continue;
+                if (x[q] & (LB_PREFIX | LB_COUNT)) sum += x[q] & LB_MASK;
+                if (x[q] & LB_PREFIX)
+                    stop = -1;
+                else if (!(x[q] & LB_COUNT))
+                    stop = jb - q;
+            }
+            lb_part[looker][dg] = sum;
+            lb_stop[looker][dg] = stop;
+        }
+        __syncthreads();
+        bool more = false;
+        if (threadIdx.x < 256 && j0 >= 0) {
+            uint32_t e = lb_excl[dg];
+            int next = j0 - 16 * W;
+#pragma unroll
+            for (int ww = 0; ww < W; ww++) {
+                e += lb_part[ww][dg];
+                const int st = lb_stop[ww][dg];
+                if (st != -2) {
+                    next = st; // -1 (done) or the tile to wait for
                     break;
                 }
             }
-            if (gave_up && err) atomicOr(err, ERR_WAIT);
-            lb_store(me, LB_PREFIX | ((excl + run) & LB_MASK));
+            if (next >= 0 && global_ns() - t0 > 1000000000ull) {
+                gave_up = true; // 1 s: a predecessor never published
+                next = -1;
+            }
+            lb_excl[dg] = e;
+            lb_next[dg] = next;
+            more = next >= 0;
         }
-        gbase[d] = aux[SORT_AUX_BASE + pass * 256 + d] + excl;
+        if (!__syncthreads_or(more)) break;
+    }
+    if (gave_up && err) atomicOr(err, ERR_WAIT);
+    if (threadIdx.x < 256) {
+        const uint32_t excl = lb_excl[dg];
+        if (tile > 0) lb_store(status + (size_t) tile * 256 + dg, LB_PREFIX | ((excl + run) & LB_MASK));
+        gbase[dg] = aux[SORT_AUX_BASE + pass * 256 + dg] + excl;
     }
     const uint32_t incl = block_incl_scan(run, wt, &tot); // threads >= 256 add 0
     if (threadIdx.x < 256) lbase[threadIdx.x] = incl - run;
