@@ -276,7 +276,15 @@ template <class R> struct Layout : LayoutBase {
         mem.pool = opts ? opts->pool : nullptr;
         mem.s = s;
         if (rep == FA2CU_REPULSION_BH && sort_setup()) return 1;
-        if (rep == FA2CU_REPULSION_BH) climb_mode = pick_climb(n, device);
+        if (rep == FA2CU_REPULSION_BH) {
+            climb_mode = pick_climb(n, device);
+            // sort tiles: fewer than ~75 tiles of 8192 keys leave most SMs
+            // idle; measured on a GB300 (sort of one iteration, ms, tiles of
+            // 256 / 512 / 1024 threads): 1e5 keys 0.050 / 0.051 / 0.060;
+            // 3e5 0.054 / 0.054 / 0.066; 1e6 0.092 / 0.077 / 0.070; 3e6
+            // 0.178 / 0.164 / 0.163
+            ss.tile_threads = n < 600000 ? 512 : 1024;
+        }
         if (rep == FA2CU_REPULSION_EXACT) {
             int sms = 0;
             cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
