@@ -76,105 +76,7 @@ enum { BP_CODES, BP_SORT, BP_TREE, BP_SUMS, BP_REPULSION, BP_ATTRACTION, BP_TOTA
 
 // ---- block-level building blocks ----------------------------------------------
 
-// Stable LSD radix sort (4 passes of 8 bits) of n (key, value) pairs by key,
-// by one block of W warps. Warp w owns the contiguous chunk
-// [w C, min(n, (w+1) C)), C a multiple of 32, and reads it in rounds of 32 in
-// order; per pass each warp counts its digits, the block turns the counts into
-// offsets (digits in order, warps in order within a digit), and each warp
-// scatters its chunk with ranks from lane matching. Ping-pong through kb / vb;
-// the result is back in key / val.
-template <int W>
-__device__ void block_sort_pairs(int n, uint32_t *key, uint32_t *val, uint32_t *kb,
-                                 uint32_t *vb, uint32_t (*cnt)[256], uint32_t *base)
-{
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const int chunk = ((n + 32 * W - 1) / (32 * W)) * 32;
-    const int lo = min(n, w * chunk), hi = min(n, lo + chunk);
-    unsigned lt;
-    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(lt));
-    for (int pass = 0; pass < 4; pass++) {
-        const int shift = 8 * pass;
-        for (int d = threadIdx.x; d < W * 256; d += blockDim.x) (&cnt[0][0])[d] = 0;
-        __syncthreads();
-        for (int b = lo; b < hi; b += 32) {
-            const int i = b + lane;
-            const bool valid = i < hi;
-            const unsigned act = __ballot_sync(0xffffffffu, valid);
-            if (valid) {
-                const unsigned d = (key[i] >> shift) & 255u;
-                const unsigned peers = match_digit8(act, d);
-                if ((peers & lt) == 0) cnt[w][d] += __popc(peers);
-            }
-            __syncwarp();
-        }
-        __syncthreads();
-        // per digit: exclusive prefix over the warps, then over the digits
-        if (threadIdx.x < 256) {
-            uint32_t run = 0;
-            for (int ww = 0; ww < W; ww++) {
-                const uint32_t c = cnt[ww][threadIdx.x];
-                cnt[ww][threadIdx.x] = run;
-                run += c;
-            }
-            base[threadIdx.x] = run;
-        }
-        __syncthreads();
-        if (w == 0) { // 8 digits per lane
-            uint32_t v[8], s = 0;
-            for (int q = 0; q < 8; q++) {
-                v[q] = base[lane * 8 + q];
-                s += v[q];
-            }
-            uint32_t incl = s;
-            for (int o = 1; o < 32; o <<= 1) {
-                const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
-                if (lane >= o) incl += t;
-            }
-            uint32_t run = incl - s;
-            for (int q = 0; q < 8; q++) {
-                base[lane * 8 + q] = run;
-                run += v[q];
-            }
-        }
-        __syncthreads();
-        if (threadIdx.x < 256)
-            for (int ww = 0; ww < W; ww++) cnt[ww][threadIdx.x] += base[threadIdx.x];
-        __syncthreads();
-        for (int b = lo; b < hi; b += 32) {
-            const int i = b + lane;
-            const bool valid = i < hi;
-            const unsigned act = __ballot_sync(0xffffffffu, valid);
-            uint32_t k = 0, v = 0, prior = 0, cntp = 0, r = 0;
-            unsigned d = 0;
-            if (valid) {
-                k = key[i];
-                v = val[i];
-                d = (k >> shift) & 255u;
-                const unsigned peers = match_digit8(act, d);
-                r = __popc(peers & lt);
-                cntp = __popc(peers);
-                prior = cnt[w][d];
-            }
-            __syncwarp();
-            if (valid) {
-                if (r == 0) cnt[w][d] = prior + cntp;
-                const uint32_t at = prior + r;
-                if (at < (uint32_t) n) { // always, for consistent counts
-                    kb[at] = k;
-                    vb[at] = v;
-                }
-            }
-            __syncwarp();
-        }
-        __syncthreads();
-        uint32_t *t = key;
-        key = kb;
-        kb = t;
-        t = val;
-        val = vb;
-        vb = t;
-    }
-}
+// (block_sort_pairs, the one-block radix sort, is in sort_tree.cuh)
 
 // Sum over the block in a fixed order (per thread, per warp by shuffles, over
 // the warps by thread 0); the result is valid in thread 0.
@@ -447,7 +349,7 @@ k_batch(int ngraphs, BatchGraph *graphs, const int *queue, int *next, int iterat
             // FP64 up to SERIAL_TOTALS_MAX nodes serially in node order (the
             // reference's order, as the single-graph path), else per thread
             // and over the block
-            const bool serial = sizeof(R) == 8 && n <= SERIAL_TOTALS_MAX;
+            const bool serial = serial_totals<R>(n);
             double ts = 0.0, tt = 0.0;
             for (int i = tid; i < n; i += T) {
                 const R2 a = f[i], b = fold[i];

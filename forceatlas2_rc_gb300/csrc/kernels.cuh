@@ -1061,12 +1061,18 @@ __device__ inline void update_speed_dev(SpeedState *st, double tsw, double ttr)
     st->efficiency = eff;
 }
 
-// Up to this many nodes the totals are summed serially in node order, the
-// reference's order (src/forceatlas2.c:770-775): in double precision the
-// speed, hence the whole trajectory, is then the reference's bit for bit.
-// Beyond, a fixed-order tree with compensation (a serial sum would cost
-// more than the rest of the iteration).
+// In the FP64 path, up to this many nodes the totals are summed serially in
+// node order, the reference's order (src/forceatlas2.c:770-775): the speed,
+// hence the whole trajectory, is then the reference's bit for bit. Beyond,
+// and always in the FP32 path (whose forces differ from the reference's in
+// any case), a fixed-order tree: float-float in FP32, with compensation in
+// FP64. A serial chain of double additions costs about 70 ns an addition
+// on a GB300 (0.28 ms an iteration at 2000 nodes).
 constexpr int SERIAL_TOTALS_MAX = 2048;
+template <class R> __host__ __device__ constexpr bool serial_totals(int n)
+{
+    return sizeof(R) == 8 && n <= SERIAL_TOTALS_MAX;
+}
 
 // Per-thread sums of swinging and traction over the nodes that can move:
 // float-float in the FP32 path, double in the FP64 path.
@@ -1089,7 +1095,7 @@ __device__ __forceinline__ void swing_node(int i, int n, const typename RT<R>::R
     const R s = m * fsqrt(sx * sx + sy * sy);
     const R t = R(0.5) * m * fsqrt(tx * tx + ty * ty);
     sw[i] = s;
-    if (n <= SERIAL_TOTALS_MAX) tr[i] = t;
+    if (serial_totals<R>(n)) tr[i] = t;
     if (fixed && fixed[i]) return;
     if constexpr (sizeof(R) == 4) {
         acc.s = ff_add(acc.s, ff_from((float) s));
@@ -1162,12 +1168,24 @@ __device__ __forceinline__ void swing_finish(SwingAcc<R> acc, int n, const uint8
     if (!last) return;
     __threadfence();
     double tsw = 0.0, ttr = 0.0;
-    if (n <= SERIAL_TOTALS_MAX) {
+    if (serial_totals<R>(n)) {
+        // the block stages the nodes' values in shared memory (dynamic, 2n
+        // reals; a fixed node's as +0, which leaves a sum unchanged), then
+        // one thread adds them in node order: the chain waits on the adds
+        // only, not on a load per node
+        extern __shared__ __align__(16) unsigned char serial_smem[];
+        R *ssw = reinterpret_cast<R *>(serial_smem), *str = ssw + n;
+        for (int i = threadIdx.x; i < n; i += blockDim.x) {
+            const bool skip = fixed && fixed[i];
+            ssw[i] = skip ? R(0) : __ldcg(sw + i);
+            str[i] = skip ? R(0) : __ldcg(tr + i);
+        }
+        __syncthreads();
         if (threadIdx.x == 0) {
+#pragma unroll 8
             for (int i = 0; i < n; i++) {
-                if (fixed && fixed[i]) continue;
-                tsw = __dadd_rn(tsw, (double) __ldcg(sw + i));
-                ttr = __dadd_rn(ttr, (double) __ldcg(tr + i));
+                tsw = __dadd_rn(tsw, (double) ssw[i]);
+                ttr = __dadd_rn(ttr, (double) str[i]);
             }
         }
     } else if constexpr (sizeof(R) == 4) {

@@ -68,6 +68,7 @@ template <class R> struct Layout : LayoutBase {
     int any_fixed = 0;
     int walk = WALK_THREAD;
     int climb_mode = 1; // leaves per aggregate thread (negative: interleaved)
+    bool block_sort = false; // few keys: the one-block sort
 
     // Leaves per thread of the tree's climb, from the ratio x of leaves to
     // the threads the device holds at once (2048 per SM in float). Measured
@@ -146,7 +147,7 @@ template <class R> struct Layout : LayoutBase {
         mass = mem.get<R>(nn);
         size = adjust ? mem.get<R>(nn) : nullptr;
         sw = mem.get<R>(nn);
-        trac = n <= SERIAL_TOTALS_MAX ? mem.get<R>(nn) : nullptr;
+        trac = serial_totals<R>(n) ? mem.get<R>(nn) : nullptr;
         fixed = any_fixed ? mem.get<uint8_t>(nn) : nullptr;
         inc_off = mem.get<int>(nn + 1);
         inc = mem.get<Inc<R>>((size_t) ninc);
@@ -284,6 +285,7 @@ template <class R> struct Layout : LayoutBase {
             // 3e5 0.054 / 0.054 / 0.066; 1e6 0.092 / 0.077 / 0.070; 3e6
             // 0.178 / 0.164 / 0.163
             ss.tile_threads = n < 600000 ? 512 : 1024;
+            block_sort = n <= SORT_BLOCK_MAX;
         }
         if (rep == FA2CU_REPULSION_EXACT) {
             int sms = 0;
@@ -377,12 +379,22 @@ template <class R> struct Layout : LayoutBase {
     // Morton codes, with the sort's digit histograms in the same launch
     void launch_build()
     {
-        sort_prepare(s, ss);
         const int nb = std::min(ceil_div(n, 256), 152 * 4);
+        if (block_sort) { // the one-block sort counts its own digits
+            k_morton<R><<<nb, 256, 0, s>>>(n, pos, quant, key, order, nullptr, nullptr, 0);
+            return;
+        }
+        sort_prepare(s, ss);
         k_morton<R><<<nb, 256, 0, s>>>(n, pos, quant, key, order, ss.digit_total, ss.counts,
                                        sort_status_words(n, 4));
     }
-    void launch_sort() { sort_pairs(s, n, key, order, ss, /*hist_ready=*/true); }
+    void launch_sort()
+    {
+        if (block_sort)
+            sort_pairs_block(s, n, key, order, ss);
+        else
+            sort_pairs(s, n, key, order, ss, /*hist_ready=*/true);
+    }
     void launch_tree()
     {
         k_gather_karras<R><<<ceil_div(n, 256), 256, 0, s>>>(n, adjust, order, pos, mass, size,
@@ -474,7 +486,9 @@ template <class R> struct Layout : LayoutBase {
     // update (an iteration's second half before the displacement).
     void launch_attraction_swing()
     {
-        k_attract_swing<R><<<ceil_div(n, 256), 256, 0, s>>>(
+        // serial totals: the last block stages 2n reals
+        const size_t smem = serial_totals<R>(n) ? 2 * (size_t) n * sizeof(R) : 0;
+        k_attract_swing<R><<<ceil_div(n, 256), 256, smem, s>>>(
             n, gravity, strong, linlog, adjust, pos, mass, size, inc_off, inc, f, fold, fixed, sw,
             trac, swing_partial, (unsigned *) (status + ST_TICKET_SWING), st, status);
     }
@@ -693,6 +707,14 @@ template <class R> struct Layout : LayoutBase {
     {
         if (!strcmp(name, "sort_threads") && (value == 256 || value == 512 || value == 1024)) {
             ss.tile_threads = (int) value;
+            return recapture();
+        }
+        if (!strcmp(name, "sort_block") && (value == 0 || value == 1)) {
+            if (value == 1 && n > SORT_BLOCK_MAX) {
+                set_message("the one-block sort handles at most %d keys", SORT_BLOCK_MAX);
+                return 1;
+            }
+            block_sort = value == 1;
             return recapture();
         }
         if (!strcmp(name, "climb") &&

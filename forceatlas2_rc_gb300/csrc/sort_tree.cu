@@ -249,6 +249,21 @@ static void onesweep_pass(cudaStream_t s, int n, int pass, const uint32_t *kin,
         n, pass, kin, vin, kout, vout, w.counts + (size_t) pass * 256 * nb, w.digit_total, w.err);
 }
 
+__global__ void __launch_bounds__(1024)
+k_sort_block(int n, uint32_t *__restrict__ key, uint32_t *__restrict__ val,
+             uint32_t *__restrict__ kb, uint32_t *__restrict__ vb)
+{
+    __shared__ uint32_t cnt[32][256];
+    __shared__ uint32_t base[256];
+    block_sort_pairs<32>(n, key, val, kb, vb, cnt, base);
+}
+
+void sort_pairs_block(cudaStream_t s, int n, uint32_t *key, uint32_t *val,
+                      const SortScratch &w)
+{
+    k_sort_block<<<1, 1024, 0, s>>>(n, key, val, w.key_b, w.val_b);
+}
+
 size_t sort_scratch_counts(int n) { return 4 * 256 * (size_t) ceil_div(n, SORT_TILE); }
 
 size_t sort_status_words(int n, int passes) { return (size_t) passes * 256 * ceil_div(n, SORT_TILE); }

@@ -46,10 +46,117 @@ int sort_setup();
 void sort_pairs(cudaStream_t s, int n, uint32_t *key, uint32_t *val,
                 const SortScratch &w, bool hist_ready = false);
 
+// The same sort by a single block of 1024 threads (block_sort_pairs, four
+// passes in one launch): for few keys, where the passes' launches and
+// look-backs cost more than the work. Scratch: key_b / val_b of w.
+constexpr int SORT_BLOCK_MAX = 4096;
+void sort_pairs_block(cudaStream_t s, int n, uint32_t *key, uint32_t *val,
+                      const SortScratch &w);
+
 // Clears the histograms and tickets (before the histogram pass).
 void sort_prepare(cudaStream_t s, const SortScratch &w);
 // Look-back words the histogram pass clears, for n keys and `passes` digits.
 size_t sort_status_words(int n, int passes);
+
+// Stable LSD radix sort (4 passes of 8 bits) of n (key, value) pairs by key,
+// by one block of W warps. Warp w owns the contiguous chunk
+// [w C, min(n, (w+1) C)), C a multiple of 32, and reads it in rounds of 32 in
+// order; per pass each warp counts its digits, the block turns the counts into
+// offsets (digits in order, warps in order within a digit), and each warp
+// scatters its chunk with ranks from lane matching. Ping-pong through kb / vb;
+// the result is back in key / val.
+template <int W>
+__device__ void block_sort_pairs(int n, uint32_t *key, uint32_t *val, uint32_t *kb,
+                                 uint32_t *vb, uint32_t (*cnt)[256], uint32_t *base)
+{
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int chunk = ((n + 32 * W - 1) / (32 * W)) * 32;
+    const int lo = min(n, w * chunk), hi = min(n, lo + chunk);
+    unsigned lt;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(lt));
+    for (int pass = 0; pass < 4; pass++) {
+        const int shift = 8 * pass;
+        for (int d = threadIdx.x; d < W * 256; d += blockDim.x) (&cnt[0][0])[d] = 0;
+        __syncthreads();
+        for (int b = lo; b < hi; b += 32) {
+            const int i = b + lane;
+            const bool valid = i < hi;
+            const unsigned act = __ballot_sync(0xffffffffu, valid);
+            if (valid) {
+                const unsigned d = (key[i] >> shift) & 255u;
+                const unsigned peers = match_digit8(act, d);
+                if ((peers & lt) == 0) cnt[w][d] += __popc(peers);
+            }
+            __syncwarp();
+        }
+        __syncthreads();
+        // per digit: exclusive prefix over the warps, then over the digits
+        if (threadIdx.x < 256) {
+            uint32_t run = 0;
+            for (int ww = 0; ww < W; ww++) {
+                const uint32_t c = cnt[ww][threadIdx.x];
+                cnt[ww][threadIdx.x] = run;
+                run += c;
+            }
+            base[threadIdx.x] = run;
+        }
+        __syncthreads();
+        if (w == 0) { // 8 digits per lane
+            uint32_t v[8], s = 0;
+            for (int q = 0; q < 8; q++) {
+                v[q] = base[lane * 8 + q];
+                s += v[q];
+            }
+            uint32_t incl = s;
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += t;
+            }
+            uint32_t run = incl - s;
+            for (int q = 0; q < 8; q++) {
+                base[lane * 8 + q] = run;
+                run += v[q];
+            }
+        }
+        __syncthreads();
+        if (threadIdx.x < 256)
+            for (int ww = 0; ww < W; ww++) cnt[ww][threadIdx.x] += base[threadIdx.x];
+        __syncthreads();
+        for (int b = lo; b < hi; b += 32) {
+            const int i = b + lane;
+            const bool valid = i < hi;
+            const unsigned act = __ballot_sync(0xffffffffu, valid);
+            uint32_t k = 0, v = 0, prior = 0, cntp = 0, r = 0;
+            unsigned d = 0;
+            if (valid) {
+                k = key[i];
+                v = val[i];
+                d = (k >> shift) & 255u;
+                const unsigned peers = match_digit8(act, d);
+                r = __popc(peers & lt);
+                cntp = __popc(peers);
+                prior = cnt[w][d];
+            }
+            __syncwarp();
+            if (valid) {
+                if (r == 0) cnt[w][d] = prior + cntp;
+                const uint32_t at = prior + r;
+                if (at < (uint32_t) n) { // always, for consistent counts
+                    kb[at] = k;
+                    vb[at] = v;
+                }
+            }
+            __syncwarp();
+        }
+        __syncthreads();
+        uint32_t *t = key;
+        key = kb;
+        kb = t;
+        t = val;
+        val = vb;
+        vb = t;
+    }
+}
 
 // Block-wide inclusive scan of one value per thread (blockDim.x <= 1024).
 __device__ __forceinline__ uint32_t block_incl_scan(uint32_t v, uint32_t *warp_tot,
