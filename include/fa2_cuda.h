@@ -75,10 +75,21 @@ int fa2cu_layout_tree(fa2cu_layout *L, const double *pos, uint32_t *key,
  * the current positions (an instrumented, untimed variant). */
 int fa2cu_layout_traversal_counts(fa2cu_layout *L, double counts[2]);
 
-/* Set a tuning option of the layout: "walk" = 1 for one independent
- * Barnes-Hut walk per thread (default), 0 for the warp-synchronous walk
- * (lanes walk together, keeping their own decisions). Both give identical
- * forces. */
+/* Set a tuning option of the layout (every choice gives identical results;
+ * nonzero and a message for an unknown name or value):
+ *   "walk"         Barnes-Hut walk: 1 one independent walk per thread
+ *                  (default), 0 warp-synchronous (lanes walk together,
+ *                  keeping their own decisions), 2 the per-thread walk
+ *                  compiled without its register bound, 3 / 4 two / four
+ *                  Morton neighbours per thread;
+ *   "climb"        leaves per thread of the bottom-up sums: 1, 2, 4 or 8
+ *                  contiguous, -2 or -4 interleaved over the warp (default:
+ *                  1 below one wave of threads, else 2 in float, 4 in
+ *                  double);
+ *   "sort_threads" 256, 512 or 1024 threads per sort tile (default: 512
+ *                  below 600000 nodes, else 1024);
+ *   "sort_block"   1: the one-block sort (at most 4096 nodes; default there),
+ *                  0: the tiled sort. */
 int fa2cu_layout_option(fa2cu_layout *L, const char *name, double value);
 
 /* Bytes of device memory held by the layout. */
