@@ -343,6 +343,7 @@ template <class R> struct Layout : LayoutBase {
         // whose reduction takes a ticket)
         FA2_TRY(cudaMemsetAsync(fold, 0, (size_t) n * sizeof(R2), s), "cudaMemset", 1);
         FA2_TRY(cudaMemsetAsync(status, 0, ST_COUNT * sizeof(int), s), "cudaMemset", 1);
+        if (repulsion == FA2CU_REPULSION_BH) sort_prepare(s, ss);
         if (set_positions(xy0)) return 1;
         SpeedState h{};
         h.speed = 1.0;
@@ -384,7 +385,9 @@ template <class R> struct Layout : LayoutBase {
             k_morton<R><<<nb, 256, 0, s>>>(n, pos, quant, key, order, nullptr, nullptr, 0);
             return;
         }
-        sort_prepare(s, ss);
+        // the histograms, done counter and tickets start at zero: cleared at
+        // open, then left at zero by the Morton kernel's last block for the
+        // next sort (no memset in the iteration)
         k_morton<R><<<nb, 256, 0, s>>>(n, pos, quant, key, order, ss.digit_total, ss.counts,
                                        sort_status_words(n, 4));
     }

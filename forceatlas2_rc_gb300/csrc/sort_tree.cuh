@@ -27,9 +27,9 @@ constexpr int SORT_AUX_HIST = 0, SORT_AUX_BASE = 1024, SORT_AUX_TICKET = 2048,
 // of each pass (4 x 256 per tile) and the auxiliary words; `err` (may be
 // null) receives ERR_WAIT if a look-back wait ever gives up.
 struct SortScratch {
-    uint32_t *key_b, *val_b; // n each
-    uint32_t *counts;        // sort_scratch_counts(n)
-    uint32_t *digit_total;   // SORT_AUX
+    uint32_t *key_b = nullptr, *val_b = nullptr; // n each
+    uint32_t *counts = nullptr;                  // sort_scratch_counts(n)
+    uint32_t *digit_total = nullptr;             // SORT_AUX
     int *err = nullptr;
     int tile_threads = 1024; // threads of a scatter block (tile = 8 keys each)
 };
