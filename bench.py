@@ -47,7 +47,8 @@ WORKLOAD = ("SBM n=1,000,000, 1000 power-law blocks (exp 2.1), deg_in 12, "
 # kernels of one Barnes-Hut iteration: morton (with the sort's histograms),
 # 4 sort scatter passes, gather + karras, aggregate, traverse, attraction +
 # swing totals + speed update, apply (with the next iteration's bounding
-# box), and one memset of the sort's counters
+# box); no memset (the sort's counters are left at zero by the Morton
+# kernel)
 LAUNCHES_PER_ITER = 10
 # Barnes-Hut walks (fa2cu_layout_option "walk"): identical forces
 WALKS = {"warp": 0, "thread": 1, "wide": 2, "pair": 3, "quad": 4}
