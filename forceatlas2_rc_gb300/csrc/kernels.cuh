@@ -503,20 +503,23 @@ __device__ __forceinline__ void climb(int k, int n, const typename RT<R>::R4 *ps
             return;
         }
         if (arrive<CTA>(visits + r) == 0) return;
+        // the region's topology first (its links are known before its sums)
         const int2 c = child[r];
-        if (c.x < 0 || c.y < 0 || c.x >= nl + n || c.y >= nl + n) {
+        const int2 rg = range[r];
+        if (c.x < 0 || c.y < 0 || c.x >= nl + n || c.y >= nl + n || rg.y < 0 || rg.y >= n) {
             atomicOr(status + ST_ERROR, ERR_BOUNDS);
             return;
         }
+        // a region of at most 8 nodes is never opened: its left link
+        // carries its packed range instead (negative)
+        const int2 links =
+            make_int2(rg.y - rg.x >= 8 ? c.x : bucket_pack(rg.x, rg.y), rope[rg.y]);
         const Agg<R> a = c.x >= nl ? leaf_agg(psort[c.x - nl]) : load_agg_cg(agg + c.x);
         const Agg<R> b = c.y >= nl ? leaf_agg(psort[c.y - nl]) : load_agg_cg(agg + c.y);
         const Agg<R> q = agg_combine(a, b);
         agg[r] = q;
-        const int2 rg = range[r];
         rec_c[r] = agg_record(q);
-        // a region of at most 8 nodes is never opened: its left link
-        // carries its packed range instead (negative)
-        rec_t[r] = make_int2(rg.y - rg.x >= 8 ? c.x : bucket_pack(rg.x, rg.y), rope[rg.y]);
+        rec_t[r] = links;
         r = parent[r];
     }
 }
@@ -554,6 +557,7 @@ k_aggregate_multi(int n, const typename RT<R>::R4 *__restrict__ psort,
             int *__restrict__ status)
 {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
+#pragma unroll 1
     for (int q = 0; q < P; q++) {
         const int k = CONTIG ? t * P + q : ((t >> 5) * P + q) * 32 + (t & 31);
         if (k < n)
