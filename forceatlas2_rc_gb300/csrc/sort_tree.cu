@@ -5,13 +5,16 @@
 //   hist4    one pass over the keys: the 256-bin histogram of every digit
 //            (per-warp shared-memory counters, summed over the warps and
 //            added to the global counts); the last block turns them into
-//            digit bases;
-//   onesweep one launch per digit: each block takes the next tile of 2048
-//            keys, ranks them stably (lanes, rounds and warps in order),
-//            publishes its per-digit counts, adds those of the tiles before
-//            it (decoupled look-back, bounded in time), stages the keys by
-//            digit in shared memory and writes runs of equal digits to
-//            consecutive global positions.
+//            digit bases (the Morton kernel does the same while it makes
+//            the keys);
+//   onesweep one launch per digit: each block takes the next tile of 8
+//            keys per thread (256, 512 or 1024 threads), ranks them stably
+//            (lanes, rounds and warps in order), publishes its per-digit
+//            counts, adds those of the tiles before it (decoupled look-back,
+//            bounded in time), stages the keys by digit in shared memory and
+//            writes runs of equal digits to consecutive global positions;
+//   block    up to a few thousand keys: one block sorts all four digits in
+//            one launch (block_sort_pairs).
 #include <algorithm>
 
 #include "sort_tree.cuh"
@@ -59,9 +62,10 @@ __device__ __forceinline__ uint32_t lb_load(const uint32_t *p)
 // in launch order, so a block only ever waits for tiles of blocks that
 // started before it), ranks its keys stably (warp-contiguous chunks, lanes
 // and rounds in order, warp matching), publishes its digit counts, adds its
-// predecessors' (look-back in windows of 16 tiles, bounded in time) and
-// scatters through shared memory in runs of equal digits. Dynamic shared
-// memory: per-warp digit counters, then the staged keys and values.
+// predecessors' (look-back: T/256 lookers per digit read 16 tiles each per
+// round; bounded in time) and scatters through shared memory in runs of
+// equal digits. Dynamic shared memory: per-warp digit counters, then the
+// staged keys and values.
 template <int T>
 __global__ void __launch_bounds__(T)
 k_sort_onesweep(int n, int pass, const uint32_t *__restrict__ kin,
