@@ -843,7 +843,7 @@ def main():
                 "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, "
                                   "one launch (profiles/kernels_sbm1m_full.md)",
                 "kernel": {"warp": "k_traverse_warp<float, 0>",
-                           "thread": "k_traverse<float, 0, 6>",
+                           "thread": "k_traverse<float, 0, 8>",
                            "wide": "k_traverse<float, 0, 1>",
                            "pair": "k_traverse_multi<float, 0, 2>",
                            "quad": "k_traverse_multi<float, 0, 4>"}[args.walk],

@@ -24,7 +24,8 @@ void set_cuda_error(const char *what, cudaError_t e);
     } while (0)
 
 // Barnes-Hut walk variants (all give identical forces): warp-synchronous;
-// one walk per thread at 6 blocks of 256 per SM (<= 40 registers); one walk
+// one walk per thread at 8 blocks of 256 per SM (<= 32 registers; 6 and <= 40
+// with prevent_overlap or in double); one walk
 // per thread with the registers the compiler wants; one thread walking for
 // two or four Morton neighbours at once.
 enum {

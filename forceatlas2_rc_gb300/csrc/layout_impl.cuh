@@ -446,9 +446,11 @@ template <class R> struct Layout : LayoutBase {
                 if (adjust)
                     k_traverse<R, true, 6><<<ceil_div(n, 256), 256, 0, s>>>(
                         n, scaling, theta2, theta2d, psort, rec_c, rec_t, agg, rope, order, f, status);
-                else
-                    k_traverse<R, false, 6><<<ceil_div(n, 256), 256, 0, s>>>(
-                        n, scaling, theta2, theta2d, psort, rec_c, rec_t, agg, rope, order, f, status);
+                else // float: 8 blocks per SM (0.597 against 0.619 ms at 6, 10^6 nodes)
+                    k_traverse<R, false, sizeof(R) == 4 ? 8 : 6>
+                        <<<ceil_div(n, 256), 256, 0, s>>>(n, scaling, theta2, theta2d, psort,
+                                                          rec_c, rec_t, agg, rope, order, f,
+                                                          status);
             } else if (walk == WALK_PAIR) {
                 const int grid = ceil_div(ceil_div(n, 2), 256);
                 if (adjust)
