@@ -57,7 +57,7 @@ WALKS = {"warp": 0, "thread": 1, "wide": 2, "pair": 3, "quad": 4}
 TRAVERSE_HBM_BYTES_PER_NODE = 28
 # DRAM bytes (read + write) of one traversal launch on this workload, from
 # one ncu capture (profiles/kernels_sbm1m_full.md)
-TRAVERSE_DRAM_BYTES = 45.94e6 + 0.90e6
+TRAVERSE_DRAM_BYTES = 45.95e6 + 0.66e6
 
 
 def make_workload(small: bool = False):
