@@ -68,6 +68,7 @@ def load(build_if_missing: bool = False):
         "fa2cu_build_info": (C.c_char_p, []),
         "fa2cu_morton_order_noalloc": (C.c_int, [C.c_int, C.c_void_p, C.c_void_p,
                                                  C.c_void_p, C.c_void_p]),
+        "fa2cu_noalloc_status": (C.c_int, [C.c_void_p]),
         "fa2cu_batch_open": (C.c_void_p, [C.POINTER(FullParams), C.c_int,
                                           C.POINTER(P_D), C.c_int, C.c_int]),
         "fa2cu_batch_iterate": (C.c_int, [C.c_void_p, C.c_int]),
@@ -122,6 +123,7 @@ EXPORTED = (
     "fa2cu_layout_traversal_counts", "fa2cu_layout_option",
     "fa2cu_layout_bytes",
     "fa2cu_layout_close", "fa2cu_build_info", "fa2cu_morton_order_noalloc",
+    "fa2cu_noalloc_status",
     "fa2cu_batch_open", "fa2cu_batch_iterate", "fa2cu_batch_sync",
     "fa2cu_batch_positions", "fa2cu_batch_speed", "fa2cu_batch_stream",
     "fa2cu_batch_phase_cycles",

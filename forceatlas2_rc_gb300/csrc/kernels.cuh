@@ -622,9 +622,10 @@ walk(int k, int n, R scaling, R theta2, double theta2d,
     // ends at -1
     const unsigned nend = (unsigned) (nl + n);
     int cur = 0, j = 0, jend = -1;
-    // a walk visits each of the 2n-1 tree nodes and each node pair at most
-    // once: more steps than that, or a link out of range, is a bug
-    const int cap = 2 * n + 64;
+    // a walk takes at most one step per region (n-1), one per single node
+    // reached as a leaf (n) and one per node pair summed (n): more steps than
+    // 3n, or a link out of range, is a bug
+    const int cap = 3 * n + 64;
     for (int step = 0;; step++) {
         if (j <= jend) {
             if (j != k) {

@@ -20,9 +20,19 @@
 //     overlap on the GPU (on different streams, or from several host
 //     threads) race and must not be issued; calls in one stream are fine;
 //   - the first call on a device looks up the array's device address there
-//     (cudaGetSymbolAddress, once per device, with that device current); that
-//     first call should come before any stream capture.
+//     (cudaGetSymbolAddress, once per device, with that device current). With
+//     CUDA's default lazy module loading, that first lookup is also when the
+//     library's device code and the array are loaded onto the device: it may
+//     allocate and synchronise, so make it up front (fa2cu_noalloc_status
+//     does only the lookup), before any stream capture;
+//   - a look-back wait of the sort that gives up (after about a second; it
+//     only happens if the GPU fails to run the sort's blocks) leaves key and
+//     order wrong; the call itself returns before the GPU runs, so it cannot
+//     say so: the error word in the array records it, and
+//     fa2cu_noalloc_status reads it back once the stream is done.
 #include <algorithm>
+#include <atomic>
+#include <cstdint>
 
 #include "kernels.cuh"
 #include "sort_tree.cuh"
@@ -41,15 +51,51 @@ constexpr size_t OFF_TOTAL = OFF_COUNTS + align256(4 * 256 * (size_t) NOALLOC_NB
 constexpr size_t OFF_PART = OFF_TOTAL + align256(SORT_AUX * 4);
 constexpr size_t OFF_BBOX = OFF_PART + align256(4 * (size_t) NOALLOC_NBBOX * 4);
 constexpr size_t OFF_QUANT = OFF_BBOX + align256(4 * 4);
+// the bounding box's arrival ticket and the sort's error word, side by side
+// so that one clear of 8 bytes starts both at zero
 constexpr size_t OFF_TICKET = OFF_QUANT + align256(6 * 8);
-constexpr size_t NOALLOC_BYTES = OFF_TICKET + align256(4);
+constexpr size_t OFF_ERR = OFF_TICKET + 4;
+constexpr size_t NOALLOC_BYTES = OFF_TICKET + align256(8);
 
 // The scratch memory of fa2cu_morton_order_noalloc (one copy per device).
 static __device__ __align__(256) unsigned char g_scratch[NOALLOC_BYTES];
 
-// Device address of g_scratch on each device, looked up on first use there.
+// Device address of g_scratch on each device, looked up on first use there
+// (atomic: host threads may make their first calls at the same time; they
+// look up the same address).
 constexpr int NOALLOC_MAX_DEVICES = 64;
-static unsigned char *g_scratch_addr[NOALLOC_MAX_DEVICES];
+static std::atomic<unsigned char *> g_scratch_addr[NOALLOC_MAX_DEVICES];
+
+// g_scratch's address on the current device (looked up once), or null with
+// the message set.
+static unsigned char *scratch_base(const char *who)
+{
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) {
+        cudaGetLastError();
+        set_message("%s: no current CUDA device", who);
+        return nullptr;
+    }
+    if (dev < 0 || dev >= NOALLOC_MAX_DEVICES) {
+        set_message("%s supports devices 0 to %d", who, NOALLOC_MAX_DEVICES - 1);
+        return nullptr;
+    }
+    unsigned char *base = g_scratch_addr[dev].load(std::memory_order_acquire);
+    if (!base) {
+        // host code may not use g_scratch itself: its name stands for a host
+        // shadow, not the device array; take the device address once
+        void *p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_scratch);
+        if (e != cudaSuccess || !p) {
+            cudaGetLastError();
+            set_cuda_error("could not locate the scratch memory", e);
+            return nullptr;
+        }
+        base = (unsigned char *) p;
+        g_scratch_addr[dev].store(base, std::memory_order_release);
+    }
+    return base;
+}
 
 } // namespace fa2cu
 
@@ -67,27 +113,21 @@ extern "C" int fa2cu_morton_order_noalloc(int n, const float *pos, uint32_t *key
         set_message("fa2cu_morton_order_noalloc: invalid (NULL) device buffer");
         return 1;
     }
-    int dev = 0;
-    FA2_TRY(cudaGetDevice(&dev), "no current CUDA device", 1);
-    if (dev < 0 || dev >= NOALLOC_MAX_DEVICES) {
-        set_message("fa2cu_morton_order_noalloc supports devices 0 to %d", NOALLOC_MAX_DEVICES - 1);
+    // the kernels read pos as float2 and write key / order as 32-bit words:
+    // a misaligned buffer would fault on the GPU, so it is refused here
+    if (((uintptr_t) pos & 7) || ((uintptr_t) key & 3) || ((uintptr_t) order & 3)) {
+        set_message("fa2cu_morton_order_noalloc: pos must be 8-byte aligned and key, order "
+                    "4-byte aligned");
         return 1;
     }
-    if (!g_scratch_addr[dev]) {
-        // host code may not use g_scratch itself: its name stands for a host
-        // shadow, not the device array; take the device address once
-        void *p = nullptr;
-        FA2_TRY(cudaGetSymbolAddress(&p, g_scratch), "could not locate the scratch memory", 1);
-        g_scratch_addr[dev] = (unsigned char *) p;
-    }
-    unsigned char *base = g_scratch_addr[dev];
+    unsigned char *base = scratch_base("fa2cu_morton_order_noalloc");
+    if (!base) return 1;
     cudaStream_t s = (cudaStream_t) stream;
     unsigned *ticket = (unsigned *) (base + OFF_TICKET);
     // the last call may have left anything here: the arrival ticket of the
-    // bounding-box reduction must start at zero (everything else is fully
-    // written before it is read)
-    FA2_TRY(cudaMemsetAsync(ticket, 0, sizeof(unsigned), s), "the computation on the GPU failed",
-            1);
+    // bounding-box reduction and the sort's error word must start at zero
+    // (everything else is fully written before it is read)
+    FA2_TRY(cudaMemsetAsync(ticket, 0, 8, s), "the computation on the GPU failed", 1);
     const int nbbox = std::min(ceil_div(n, 256), NOALLOC_NBBOX);
     const float2 *p2 = reinterpret_cast<const float2 *>(pos);
     k_bbox<float><<<nbbox, 256, 0, s>>>(n, p2, (float *) (base + OFF_PART),
@@ -101,7 +141,26 @@ extern "C" int fa2cu_morton_order_noalloc(int n, const float *pos, uint32_t *key
     w.val_b = (uint32_t *) (base + OFF_VAL_B);
     w.counts = (uint32_t *) (base + OFF_COUNTS);
     w.digit_total = (uint32_t *) (base + OFF_TOTAL);
+    w.err = (int *) (base + OFF_ERR);
     sort_pairs(s, n, key, order, w);
     FA2_TRY(cudaGetLastError(), "the computation on the GPU failed", 1);
+    return 0;
+}
+
+extern "C" int fa2cu_noalloc_status(void *stream)
+{
+    unsigned char *base = scratch_base("fa2cu_noalloc_status");
+    if (!base) return 1;
+    cudaStream_t s = (cudaStream_t) stream;
+    int err = 0;
+    // ordered after the stream's earlier work, i.e. after the last call's sort
+    FA2_TRY(cudaMemcpyAsync(&err, base + OFF_ERR, sizeof(int), cudaMemcpyDeviceToHost, s),
+            "the computation on the GPU failed", 1);
+    FA2_TRY(cudaStreamSynchronize(s), "the computation on the GPU failed", 1);
+    if (err & ERR_WAIT) {
+        set_message("the computation on the GPU failed (a device wait timed out): "
+                    "the Morton order of the last call is wrong");
+        return 1;
+    }
     return 0;
 }

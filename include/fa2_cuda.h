@@ -244,13 +244,24 @@ double fa2cu_layout_footprint(int n, int ninc, int adjust, int any_fixed,
  *   key    device, n uint32: the sorted Morton codes (16 bits per axis);
  *   order  device, n uint32: node indices in Morton order, ties by index;
  *   stream the cudaStream_t to run on (NULL: the default stream).
- * 1 <= n <= 2^20, larger n is an error. Its scratch is a static device array
- * of the library (about 9 MB per GPU, held until exit) shared by every
+ * 1 <= n <= 2^20, larger n is an error. pos must be 8-byte aligned, key and
+ * order 4-byte aligned (refused otherwise). Its scratch is a static device
+ * array of the library (about 9 MB per GPU, held until exit) shared by every
  * call: calls that overlap on the GPU race. The first call on a device looks
- * the array up on that device; make it before any stream capture. Returns 0,
- * or non-zero with a message for fa2_gpu_error(). */
+ * the array up on that device, which (with CUDA's lazy module loading) also
+ * loads the library's device code and the array there and may allocate and
+ * synchronise: make it up front (fa2cu_noalloc_status does only that
+ * lookup), before any stream capture. Returns 0 once the work is queued, or
+ * non-zero with a message for fa2_gpu_error(). */
 int fa2cu_morton_order_noalloc(int n, const float *pos, uint32_t *key,
                                uint32_t *order, void *stream);
+
+/* Companion of fa2cu_morton_order_noalloc, on the current device: waits for
+ * `stream`, then returns 0 if the last call there completed, or non-zero
+ * with a message if one of its sort's bounded waits gave up (its key and
+ * order are then wrong). Also the up-front set-up of the scratch array. It
+ * allocates nothing. No counterpart in the reference. */
+int fa2cu_noalloc_status(void *stream);
 
 /* Library build description (compile flags and architecture). */
 const char *fa2cu_build_info(void);

@@ -8,8 +8,9 @@ device (the first steps of the tree build) come with all scratch memory in a
 static device array of the library. This test calls it through the C
 interface on caller-owned device buffers and checks it against the same
 step of a resident layout (fa2cu_layout_tree): keys and order bit-exact, on
-calls in a row that reuse the shared scratch. It sits in a file of its own,
-collected last.
+calls in a row that reuse the shared scratch, each followed by a clean
+fa2cu_noalloc_status (no bounded wait of the sort gave up). It sits in a
+file of its own, collected last.
 """
 import numpy as np
 import pytest
@@ -48,6 +49,7 @@ def test_noalloc_matches_layout_tree(cuda_lib, gpu):
         rc = lib.fa2cu_morton_order_noalloc(n, dpos.data_ptr(), key.data_ptr(),
                                             order.data_ptr(), stream)
         assert rc == 0, lib.fa2_gpu_error()
+        assert lib.fa2cu_noalloc_status(stream) == 0, lib.fa2_gpu_error()
         torch.cuda.synchronize(dev)
         want_key, want_order = _expected(pos)
         np.testing.assert_array_equal(key.cpu().numpy().view(np.uint32), want_key)
@@ -59,3 +61,12 @@ def test_noalloc_rejects_oversized(cuda_lib, gpu):
     rc = lib.fa2cu_morton_order_noalloc((1 << 20) + 1, 16, 16, 16, None)
     assert rc != 0
     assert b"1048576" in lib.fa2_gpu_error()
+
+
+def test_noalloc_rejects_misaligned(cuda_lib, gpu):
+    """Buffers the kernels could not address (pos not 8-byte aligned, key
+    or order not 4-byte aligned) are refused on the host; nothing runs."""
+    lib = cuda_lib
+    for pos, key, order in ((20, 16, 16), (16, 18, 16), (16, 16, 17)):
+        assert lib.fa2cu_morton_order_noalloc(100, pos, key, order, None) != 0
+        assert b"aligned" in lib.fa2_gpu_error()
