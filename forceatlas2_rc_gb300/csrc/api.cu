@@ -344,6 +344,10 @@ int fa2cu_layout_option(fa2cu_layout *L, const char *name, double value)
     }
     return L->impl->option(name, value);
 }
+int fa2cu_layout_swing(fa2cu_layout *L, double *sw, double *tr)
+{
+    return L->impl->swing(sw, tr);
+}
 double fa2cu_layout_bytes(const fa2cu_layout *L) { return L->impl->bytes(); }
 void fa2cu_layout_close(fa2cu_layout *L)
 {

@@ -1100,7 +1100,7 @@ __device__ __forceinline__ void swing_node(int i, int n, const typename RT<R>::R
     const R s = m * fsqrt(sx * sx + sy * sy);
     const R t = R(0.5) * m * fsqrt(tx * tx + ty * ty);
     sw[i] = s;
-    if (serial_totals<R>(n)) tr[i] = t;
+    if (tr) tr[i] = t; // kept for the serial totals, or on request
     if (fixed && fixed[i]) return;
     if constexpr (sizeof(R) == 4) {
         acc.s = ff_add(acc.s, ff_from((float) s));
@@ -1116,20 +1116,20 @@ __device__ __forceinline__ ff2 ff_shfl_down(ff2 a, int o)
     return ff2{__shfl_down_sync(0xffffffffu, a.hi, o), __shfl_down_sync(0xffffffffu, a.lo, o)};
 }
 
-// The end of the totals, by every thread of every block of the kernel: the
-// block's sums in a fixed tree order (float-float or compensated double), a
-// partial per block, then the last block to finish sums the partials in a
-// fixed order (float-float in the FP32 path, the partials' pairs being
-// (hi, lo) floats; compensated double in the FP64 path) -- or, up to
-// SERIAL_TOTALS_MAX nodes, sums the nodes serially in node order in double
-// (the reference's order) -- and updates Gephi's adaptive speed in double.
+// The end of the totals, by every thread of every block of the kernel: each
+// warp's sums (float-float in the FP32 path, whose 48 bits hold the sum of
+// 32 floats to ~1e-14; double in the FP64 path), then in double from there
+// on: the warps' sums by thread 0 with Neumaier compensation into a partial
+// per block, then the last block to finish sums the partials with Neumaier
+// compensation, in a fixed order -- or, up to SERIAL_TOTALS_MAX nodes in the
+// FP64 path, sums the nodes serially in node order (the reference's order)
+// -- and updates Gephi's adaptive speed in double.
 template <class R>
 __device__ __forceinline__ void swing_finish(SwingAcc<R> acc, int n, const uint8_t *fixed,
                                              const R *sw, const R *tr, double2 *partial,
                                              unsigned *ticket, SpeedState *st, int *status)
 {
     __shared__ double ss[32], st_[32];
-    __shared__ ff2 fss[32], fst[32];
     __shared__ int last;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
     if constexpr (sizeof(R) == 4) {
@@ -1137,9 +1137,9 @@ __device__ __forceinline__ void swing_finish(SwingAcc<R> acc, int n, const uint8
             acc.s = ff_add(acc.s, ff_shfl_down(acc.s, o));
             acc.t = ff_add(acc.t, ff_shfl_down(acc.t, o));
         }
-        if (lane == 0) {
-            fss[w] = acc.s;
-            fst[w] = acc.t;
+        if (lane == 0) { // hi + lo is exact in double
+            ss[w] = ff_to_double(acc.s);
+            st_[w] = ff_to_double(acc.t);
         }
     } else {
         acc.ds = warp_sum(acc.ds);
@@ -1151,21 +1151,12 @@ __device__ __forceinline__ void swing_finish(SwingAcc<R> acc, int n, const uint8
     }
     __syncthreads();
     if (threadIdx.x == 0) {
-        if constexpr (sizeof(R) == 4) {
-            ff2 a = fss[0], b = fst[0];
-            for (int k = 1; k < nw; k++) {
-                a = ff_add(a, fss[k]);
-                b = ff_add(b, fst[k]);
-            }
-            reinterpret_cast<float4 *>(partial)[blockIdx.x] = make_float4(a.hi, a.lo, b.hi, b.lo);
-        } else {
-            double a = 0.0, b = 0.0, ca = 0.0, cb = 0.0;
-            for (int k = 0; k < nw; k++) {
-                neumaier(a, ca, ss[k]);
-                neumaier(b, cb, st_[k]);
-            }
-            partial[blockIdx.x] = make_double2(__dadd_rn(a, ca), __dadd_rn(b, cb));
+        double a = 0.0, b = 0.0, ca = 0.0, cb = 0.0;
+        for (int k = 0; k < nw; k++) {
+            neumaier(a, ca, ss[k]);
+            neumaier(b, cb, st_[k]);
         }
+        partial[blockIdx.x] = make_double2(__dadd_rn(a, ca), __dadd_rn(b, cb));
         __threadfence();
         last = atomicAdd(ticket, 1u) == gridDim.x - 1;
     }
@@ -1192,35 +1183,6 @@ __device__ __forceinline__ void swing_finish(SwingAcc<R> acc, int n, const uint8
                 tsw = __dadd_rn(tsw, (double) ssw[i]);
                 ttr = __dadd_rn(ttr, (double) str[i]);
             }
-        }
-    } else if constexpr (sizeof(R) == 4) {
-        // the partials: per thread (strided, fixed), per warp, over the warps
-        ff2 a = ff2{0.0f, 0.0f}, b = ff2{0.0f, 0.0f};
-        const float4 *pf = reinterpret_cast<const float4 *>(partial);
-        for (int k = threadIdx.x; k < (int) gridDim.x; k += blockDim.x) {
-            const float4 v = __ldcg(pf + k);
-            a = ff_add(a, ff2{v.x, v.y});
-            b = ff_add(b, ff2{v.z, v.w});
-        }
-        for (int o = 16; o > 0; o >>= 1) {
-            a = ff_add(a, ff_shfl_down(a, o));
-            b = ff_add(b, ff_shfl_down(b, o));
-        }
-        __syncthreads();
-        if (lane == 0) {
-            fss[w] = a;
-            fst[w] = b;
-        }
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            a = fss[0];
-            b = fst[0];
-            for (int k = 1; k < nw; k++) {
-                a = ff_add(a, fss[k]);
-                b = ff_add(b, fst[k]);
-            }
-            tsw = ff_to_double(a);
-            ttr = ff_to_double(b);
         }
     } else {
         double s1 = 0.0, c1 = 0.0, s2 = 0.0, c2 = 0.0;

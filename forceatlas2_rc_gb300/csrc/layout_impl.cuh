@@ -734,8 +734,44 @@ template <class R> struct Layout : LayoutBase {
             walk = (int) value;
             return recapture();
         }
+        if (!strcmp(name, "keep_traction") && value == 1) {
+            // per-node traction kept for fa2cu_layout_swing (the FP64 path
+            // keeps it anyway up to SERIAL_TOTALS_MAX nodes)
+            if (!trac) {
+                cudaSetDevice(device);
+                FA2_TRY(cudaStreamSynchronize(s), "the computation on the GPU failed", 1);
+                trac = mem.get<R>((size_t) n);
+                if (!trac) {
+                    set_cuda_error("could not allocate memory on the device", mem.err);
+                    return 1;
+                }
+            }
+            return recapture();
+        }
         set_message("unknown option %s = %g", name, value);
         return 1;
+    }
+
+    int swing(double *hsw, double *htr) override
+    {
+        if (htr && !trac) {
+            set_message("the per-node traction is not kept (option keep_traction)");
+            return 1;
+        }
+        cudaSetDevice(device);
+        std::vector<R> a((size_t) n), b(htr ? (size_t) n : 0);
+        FA2_TRY(cudaMemcpyAsync(a.data(), sw, (size_t) n * sizeof(R), cudaMemcpyDeviceToHost, s),
+                "could not fetch the swinging", 1);
+        if (htr)
+            FA2_TRY(cudaMemcpyAsync(b.data(), trac, (size_t) n * sizeof(R),
+                                    cudaMemcpyDeviceToHost, s),
+                    "could not fetch the traction", 1);
+        FA2_TRY(cudaStreamSynchronize(s), "could not fetch the swinging", 1);
+        for (int i = 0; i < n; i++) {
+            if (hsw) hsw[i] = (double) a[i];
+            if (htr) htr[i] = (double) b[i];
+        }
+        return 0;
     }
 
     int traversal_counts(double out[2]) override

@@ -298,6 +298,14 @@ class Layout:
         self._check(self.lib.fa2cu_layout_traversal_counts(self.h, dptr(c)))
         return dict(visits=c[0], pairs=c[1])
 
+    def swing(self, traction: bool = False):
+        """Per-node swinging (and traction, after option("keep_traction",
+        1)) of the last iteration."""
+        sw = np.zeros(self.n)
+        tr = np.zeros(self.n) if traction else None
+        self._check(self.lib.fa2cu_layout_swing(self.h, dptr(sw), dptr(tr)))
+        return (sw, tr) if traction else sw
+
     def option(self, name: str, value: float):
         """Tuning option (fa2cu_layout_option), e.g. option("walk", 1)."""
         self._check(self.lib.fa2cu_layout_option(self.h, name.encode(), float(value)))

@@ -89,8 +89,16 @@ int fa2cu_layout_traversal_counts(fa2cu_layout *L, double counts[2]);
  *   "sort_threads" 256, 512 or 1024 threads per sort tile (default: 512
  *                  below 600000 nodes, else 1024);
  *   "sort_block"   1: the one-block sort (at most 4096 nodes; default there),
- *                  0: the tiled sort. */
+ *                  0: the tiled sort;
+ *   "keep_traction" 1: keep each node's traction of the last iteration for
+ *                  fa2cu_layout_swing (n more reals on the device). */
 int fa2cu_layout_option(fa2cu_layout *L, const char *name, double value);
+
+/* Each node's swinging (sw, n doubles) and traction (tr, n doubles; needs
+ * the option keep_traction, else pass NULL) of the last iteration, the
+ * values the swing/traction totals of fa2cu_layout_speed sum (fixed nodes
+ * excluded). Either pointer may be NULL. */
+int fa2cu_layout_swing(fa2cu_layout *L, double *sw, double *tr);
 
 /* Bytes of device memory held by the layout. */
 double fa2cu_layout_bytes(const fa2cu_layout *L);

@@ -374,3 +374,29 @@ def test_climb_leaves_per_thread_give_the_same_tree(gpu, prec):
             want_f, want_xy = f, xy
         np.testing.assert_array_equal(f, want_f, err_msg=f"climb {mode}")
         np.testing.assert_array_equal(xy, want_xy, err_msg=f"climb {mode}")
+
+
+@pytest.mark.parametrize("prec,n", [("single", 200_000), ("single", 3000),
+                                    ("double", 50_000), ("double", 1500)])
+def test_totals_are_fp64_compensated(gpu, prec, n):
+    """The swing/traction totals that drive the speed controller are summed
+    in FP64 with compensation in both paths (float-float within a warp in
+    FP32, whose 48 bits hold a warp's sum): they equal the exact sum
+    (math.fsum) of the same per-node values, fixed nodes excluded, within
+    1e-12 relative (reference src/forceatlas2.c:758-777)."""
+    import math
+    n, a, b = G.barabasi_albert(n, 3, seed=8)
+    w = np.random.default_rng(4).lognormal(0.0, 0.5, len(a))
+    pos = f32(G.uniform_positions(n, 0, 1000, seed=9))
+    fixed = (np.random.default_rng(5).random(n) < 0.05).astype(np.int32)
+    with make_layout(n, a, b, w, pos, prec, theta=1.2, fixed=fixed) as L:
+        L.option("keep_traction", 1)
+        L.iterate(3)
+        L.sync()
+        sw, tr = L.swing(traction=True)
+        st = L.speed()
+    keep = fixed == 0
+    for got, vals in ((st["total_swinging"], sw[keep]), (st["total_traction"], tr[keep])):
+        want = math.fsum(vals)
+        assert want > 0
+        assert abs(got - want) <= 1e-12 * want, (got, want)
