@@ -174,25 +174,21 @@ def island_graph(n: int, mean_degree: float, island: int = 40, seed: int = 1):
     1), and every island sends 2 edges to random other islands."""
     rng = _rng(seed)
     k = max(1, -(-n // island))
-    fa, ta = [], []
-    start = 0
-    for c in range(k):
-        s = min(island, n - start)
-        if s >= 2:
-            iu, ju = np.triu_indices(s, k=1)
-            pick = rng.random(iu.size) < min(1.0, mean_degree / (island - 1))
-            fa.append(iu[pick] + start)
-            ta.append(ju[pick] + start)
-        start += s
+    sizes = np.full(k, island, dtype=np.int64)
+    sizes[-1] = n - island * (k - 1)
+    iu, ju = np.triu_indices(island, k=1)
+    # one draw per pair slot of every island; the last island keeps only the
+    # pairs of its own nodes
+    pick = rng.random((k, iu.size)) < min(1.0, mean_degree / (island - 1))
+    pick &= ju[None, :] < sizes[:, None]
+    c, q = np.nonzero(pick)
+    fa = [iu[q] + c * island]
+    ta = [ju[q] + c * island]
     if k > 1:
         src = np.repeat(np.arange(k), 2)
         dst = (src + rng.integers(1, k, src.size)) % k
-        fa.append(src * island + rng.integers(0, island, src.size) % np.minimum(
-            island, n - src * island))
-        ta.append(dst * island + rng.integers(0, island, src.size) % np.minimum(
-            island, n - dst * island))
-    if not fa:
-        return n, np.zeros(0, np.int32), np.zeros(0, np.int32)
+        fa.append(src * island + rng.integers(0, island, src.size) % sizes[src])
+        ta.append(dst * island + rng.integers(0, island, src.size) % sizes[dst])
     a, b = dedupe(n, np.concatenate(fa), np.concatenate(ta))
     return n, a, b
 

@@ -140,7 +140,9 @@ class Graph:
         other = np.concatenate([to[keep], frm[keep]])
         eidx = np.concatenate([keep, keep])
         cc = np.concatenate([c, c])
-        order = np.lexsort((eidx, owner))  # by node, then edge order
+        # by node, then edge order (each (node, edge) pair is unique: no
+        # self-loop is left)
+        order = np.argsort(owner * max(len(frm), 1) + eidx)
         self.inc_node = np.ascontiguousarray(other[order], dtype=np.int32)
         self.inc_coef = np.ascontiguousarray(cc[order], dtype=np.float64)
         self.inc_off = np.zeros(n + 1, np.int32)

@@ -195,3 +195,47 @@ def test_batch_tune_and_errors(gpu):
     bad.inc_node = np.array([500, 0], np.int32)  # a neighbour out of range
     with pytest.raises(RuntimeError):
         Batch([g, bad], [pos, pos])
+
+
+def test_batch_matches_oracle(gpu, orc):
+    """Batched FP64 graphs against the oracle directly, not against another
+    CUDA path: exact-repulsion graphs after 10 iterations against
+    C_forceatlas2 (the oracle's restatement of src/forceatlas2.c) within 1e-9
+    (the bar of test-gpu.R:34-58); Barnes-Hut graphs after 1 and after 5
+    iterations against the oracle's restatement of the all-GPU pipeline
+    (inst/opencl/pipeline.cl in double, FP64 totals) within 1e-9."""
+    exact_sizes, bh_sizes = [60, 250, 900], [1500, 3000, 9000]
+    raw = []
+    for i, n in enumerate(exact_sizes + bh_sizes):
+        n, a, b = G.erdos_renyi(n, 6.0, seed=200 + i)
+        w = np.random.default_rng(200 + i).lognormal(0.0, 0.5, len(a))
+        pos = f32(G.uniform_positions(n, -10 * np.sqrt(n), 10 * np.sqrt(n), seed=300 + i))
+        raw.append((n, a, b, w, pos))
+    gs = [Graph(n, a, b, w) for n, a, b, w, _ in raw]
+    ps = [pos for *_, pos in raw]
+    kw = dict(scaling=2.0, gravity=1.0, theta=1.2)
+    with Batch(gs, ps, precision="double", exact_below=1000, threads=512, **kw) as B:
+        B.iterate(1)
+        B.sync()
+        one = [B.positions(i) for i in range(len(gs))]
+        B.iterate(4)
+        B.sync()
+        five = [B.positions(i) for i in range(len(gs))]
+        B.iterate(5)
+        B.sync()
+        ten = [B.positions(i) for i in range(len(gs))]
+
+    def close(got, want, what):
+        np.testing.assert_allclose(got, want, rtol=1e-9, atol=1e-9 * np.abs(want).max(),
+                                   err_msg=what)
+
+    o = orc.Opts(scaling=2.0, gravity=1.0)
+    for i in range(len(exact_sizes)):
+        n, a, b, w, pos = raw[i]
+        close(ten[i], orc.layout(n, a, b, w, pos, None, None, 10, o), f"exact n={n}")
+    for i in range(len(exact_sizes), len(raw)):
+        n, a, b, w, pos = raw[i]
+        go = orc.prepare_large(n, a, b, w)
+        for iters, got in ((1, one[i]), (5, five[i])):
+            p, keep = orc.full_params(go, iterations=iters, **kw)
+            close(got, orc.pipe_run(p, pos, "d"), f"Barnes-Hut n={n}, {iters} iterations")

@@ -400,3 +400,30 @@ def test_totals_are_fp64_compensated(gpu, prec, n):
         want = math.fsum(vals)
         assert want > 0
         assert abs(got - want) <= 1e-12 * want, (got, want)
+
+
+def test_config2_ba100k_forces(gpu, orc):
+    """Config 2 at its full size: Barabasi-Albert, 100,000 nodes, m = 3,
+    weights lognormal(0, 0.5), positions U[0,1000]^2, theta 1.2. Per-step
+    forces from identical positions: FP64 within 1e-12 of the oracle's double
+    construction; FP32 within 1e-4 of FP64 and within 1e-5 of the oracle's
+    restatement of the FP32 path."""
+    n, a, b = G.barabasi_albert(100_000, 3, seed=1)
+    w = np.random.default_rng(1).lognormal(0.0, 0.5, len(a))
+    pos = f32(G.uniform_positions(n, 0.0, 1000.0, seed=3))
+    go = orc.prepare_large(n, a, b, w)
+    p, keep = orc.full_params(go, theta=1.2, scaling=2.0)
+    want_d = orc.pipe_forces(p, pos, "d")
+    with make_layout(n, a, b, w, pos, "double", theta=1.2) as L:
+        fd = L.forces(pos)
+    assert rel_err(fd, want_d) <= 1e-12
+    with make_layout(n, a, b, w, pos, "single", theta=1.2) as L:
+        ff = L.forces(pos)
+        L.iterate(20)
+        L.sync()
+        xy = L.positions()
+        ff2 = L.forces(xy)
+    assert rel_err(ff, want_d) <= 1e-4
+    assert rel_err(ff, orc.pipe_forces(p, pos, "m")) <= 1e-5
+    # and after 20 iterations of the FP32 layout, from its own positions
+    assert rel_err(ff2, orc.pipe_forces(p, xy, "d")) <= 1e-4

@@ -191,3 +191,48 @@ def test_server_least_work_first(gpu):
     np.testing.assert_array_equal(res[ids[0]][1], want_big)
     with pytest.raises(ValueError):
         Server(policy="random")
+
+
+def test_served_jobs_match_oracle(gpu, orc):
+    """One served FP64 job of each kind, submitted together, against the
+    oracle's restatement of the all-GPU pipeline (pipeline.cl in double,
+    FP64 totals) rather than another CUDA path: a Barabasi-Albert job, an SBM
+    job with linlog, a continuation from stored coordinates with
+    prevent_overlap and node sizes U[1,5], and a job that pins its top-1%
+    degree nodes. Positions after 12 iterations within 1e-9."""
+    specs = [("ba", 1800, 61, {}), ("sbm", 2000, 62, dict(linlog=True)),
+             ("ba", 1500, 63, "continuation"), ("sbm", 5000, 64, "pinned")]
+    jobs = []
+    for kind, n, seed, extra in specs:
+        if kind == "ba":
+            n, a, b = G.barabasi_albert(n, 3, seed=seed)
+        else:
+            n, a, b = G.sbm(n, max(2, n // 500), 2.1, 12.0, 2.0, seed=seed)
+        w = np.random.default_rng(seed).lognormal(0.0, 0.5, len(a))
+        g = Graph(n, a, b, w)
+        pos = f32(G.uniform_positions(n, 0.0, 1000.0, seed=seed + 1))
+        kw = dict(scaling=2.0, gravity=1.0, theta=1.2)
+        if extra == "continuation":
+            pos = single(g, pos, 30, "double", REPULSION_BH, **kw)  # stored coordinates
+            kw.update(adjust=True, size=f32(np.random.default_rng(seed).uniform(1, 5, n)))
+        elif extra == "pinned":
+            top = np.argsort(-(g.mass - 1.0), kind="stable")[:max(1, n // 100)]
+            fixed = np.zeros(n, np.int32)
+            fixed[top] = 1
+            kw["fixed"] = fixed
+        else:
+            kw.update(extra)
+        jobs.append((n, a, b, w, g, pos, kw))
+    iters = 12
+    with Server(max_jobs=4, chunk=5) as S:
+        ids = [S.submit(g, pos, iters, precision="double", **kw)
+               for n, a, b, w, g, pos, kw in jobs]
+        got = [S.wait(jid)[1] for jid in ids]
+    for k, (n, a, b, w, g, pos, kw) in enumerate(jobs):
+        go = orc.prepare_large(n, a, b, w)
+        p, keep = orc.full_params(go, iterations=iters, **kw)
+        want = orc.pipe_run(p, pos, "d")
+        np.testing.assert_allclose(got[k], want, rtol=1e-9,
+                                   atol=1e-9 * np.abs(want).max(), err_msg=f"job {k}")
+        if "fixed" in kw:
+            np.testing.assert_array_equal(got[k][kw["fixed"] == 1], pos[kw["fixed"] == 1])
