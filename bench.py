@@ -54,14 +54,9 @@ UNIT = "node-iters/s"
 WORKLOAD = ("SBM n=1,000,000, 1000 power-law blocks (exp 2.1), deg_in 12, "
             "deg_out 2, unit weights; linlog + dissuade_hubs, Barnes-Hut "
             "theta 1.2, FP32 positions/forces, FP64 speed control")
-# kernels of one Barnes-Hut iteration: morton (with the sort's histograms),
-# 4 sort scatter passes, gather + karras, aggregate, traverse, attraction +
-# swing totals + speed update, apply (with the next iteration's bounding
-# box); no memset (the sort's counters are left at zero by the Morton
-# kernel)
-LAUNCHES_PER_ITER = 10
-# Barnes-Hut walks (fa2cu_layout_option "walk"): identical forces
-WALKS = {"warp": 0, "thread": 1, "wide": 2, "pair": 3, "quad": 4}
+# Barnes-Hut walks (fa2cu_layout_option "walk"): the same regions and node
+# pairs (the deferred walk adds them up in another order)
+WALKS = {"warp": 0, "thread": 1, "wide": 2, "pair": 3, "quad": 4, "deferred": 5}
 # algorithmic HBM bytes per node of the traversal: psort record 16, order 4,
 # force write 8 (FP32)
 TRAVERSE_HBM_BYTES_PER_NODE = 28
@@ -549,6 +544,8 @@ def ba_result(args, local, work):
     kw = dict(scaling=2.0, gravity=1.0, theta=1.2, device=local)
     out = {"workload": BA_WORKLOAD, "n": n, "edges": int(len(a)), "iterations": iters}
     L = Layout(g, pos, precision="single", repulsion=REPULSION_BH, **kw)
+    # kernels of one captured iteration (fa2cu_layout_info)
+    out["launches_per_iteration"] = int(L.info("launches_per_iteration"))
     # force errors from identical positions: coordinates the FP32 path holds
     pos32 = pos.astype(np.float32).astype(np.float64)
     f0_32 = L.forces(pos32)
@@ -614,7 +611,8 @@ def run_ba(args):
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": BA_WORKLOAD, "n": r["n"], "edges": r["edges"]},
             "result": r, "e2e": r.get("e2e"), "cpu_baseline": cpu,
-            "gpu_launches": LAUNCHES_PER_ITER * r["iterations"], "clocks": r["clocks"]}
+            "gpu_launches": r["launches_per_iteration"] * r["iterations"],
+            "clocks": r["clocks"]}
     if rank == 0:
         print(json.dumps(line), flush=True)
     return 0
@@ -961,6 +959,12 @@ def headline(args, local, ws, pg):
     if args.walk != "thread":
         L.option("walk", WALKS[args.walk])
     stream = torch.cuda.ExternalStream(L.stream, device=local)
+    # kernels of one captured iteration: Morton codes (with the sort's digit
+    # histograms), 4 sort passes, gather + Karras tree, the bottom-up sums,
+    # the traversal, (the hubs' attraction, if any), attraction with the
+    # swing totals and the speed update, the displacement (with the next
+    # bounding box); no memset
+    launches = int(L.info("launches_per_iteration"))
 
     if args.profile_only:
         L.iterate(max(args.warmup, 1))
@@ -1081,7 +1085,8 @@ def headline(args, local, ws, pg):
                            "thread": "k_traverse<float, 0, 8>",
                            "wide": "k_traverse<float, 0, 1>",
                            "pair": "k_traverse_multi<float, 0, 2>",
-                           "quad": "k_traverse_multi<float, 0, 4>"}[args.walk],
+                           "quad": "k_traverse_multi<float, 0, 4>",
+                           "deferred": "k_traverse_deferred<float, 0, 8>"}[args.walk],
                 "peak_kind": f"{kind} (HBM copy)",
                 "launch_ms": ph["repulsion"],
                 "l2_request_bytes": l2_bytes,
@@ -1104,7 +1109,7 @@ def headline(args, local, ws, pg):
         "force_err_fp32_vs_fp64_start": _rel_err(f0_32, f0_64),
         "iterations_per_s": 1000.0 * args.steps / ms,
         "phase_ms": ph,
-        "gpu_launches": LAUNCHES_PER_ITER * args.steps,
+        "gpu_launches": launches * args.steps, "launches_per_iteration": launches,
         "e2e": e2e, "roofline": roofline, "cpu_baseline": None,
         "clocks": clocks,
     }
@@ -1133,7 +1138,7 @@ def main():
                          "batch: 4096 graphs in one persistent launch; "
                          "serve: the layout server on a Poisson job trace")
     ap.add_argument("--walk", default="thread",
-                    choices=["warp", "thread", "wide", "pair", "quad"],
+                    choices=["warp", "thread", "wide", "pair", "quad", "deferred"],
                     help="Barnes-Hut walk (identical forces)")
     args = ap.parse_args()
     if args.impl == "reference":

@@ -64,6 +64,7 @@ def load(build_if_missing: bool = False):
         "fa2cu_layout_traversal_counts": (C.c_int, [C.c_void_p, P_D]),
         "fa2cu_layout_option": (C.c_int, [C.c_void_p, C.c_char_p, C.c_double]),
         "fa2cu_layout_swing": (C.c_int, [C.c_void_p, P_D, P_D]),
+        "fa2cu_layout_info": (C.c_double, [C.c_void_p, C.c_char_p]),
         "fa2cu_layout_bytes": (C.c_double, [C.c_void_p]),
         "fa2cu_layout_close": (None, [C.c_void_p]),
         "fa2cu_build_info": (C.c_char_p, []),
@@ -122,6 +123,7 @@ EXPORTED = (
     "fa2cu_layout_forces", "fa2cu_layout_speed", "fa2cu_layout_stream",
     "fa2cu_layout_phase_times", "fa2cu_layout_tree",
     "fa2cu_layout_traversal_counts", "fa2cu_layout_option", "fa2cu_layout_swing",
+    "fa2cu_layout_info",
     "fa2cu_layout_bytes",
     "fa2cu_layout_close", "fa2cu_build_info", "fa2cu_morton_order_noalloc",
     "fa2cu_noalloc_status",

@@ -344,6 +344,14 @@ int fa2cu_layout_option(fa2cu_layout *L, const char *name, double value)
     }
     return L->impl->option(name, value);
 }
+double fa2cu_layout_info(fa2cu_layout *L, const char *name)
+{
+    if (!name) {
+        set_message("invalid layout information name");
+        return -1.0;
+    }
+    return L->impl->info(name);
+}
 int fa2cu_layout_swing(fa2cu_layout *L, double *sw, double *tr)
 {
     return L->impl->swing(sw, tr);

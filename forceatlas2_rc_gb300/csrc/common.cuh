@@ -34,6 +34,7 @@ enum {
     WALK_THREAD_WIDE = 2,
     WALK_PAIR = 3,
     WALK_QUAD = 4,
+    WALK_DEFERRED = 5,
 };
 
 // Nanoseconds of the GPU's global timer (bounds of every device-side wait).

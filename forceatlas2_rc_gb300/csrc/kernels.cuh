@@ -691,6 +691,113 @@ k_traverse(int n, R scaling, R theta2, double theta2d,
                                   rope, status);
 }
 
+// The walk with its node pairs deferred (FP32 path). In the walk above, a
+// warp whose lanes are partly summing node pairs and partly visiting
+// regions issues both kinds of step in nearly every iteration. Here the walk
+// visits regions only: a small region that is too close (and a single node
+// reached as a leaf) is queued as its packed sorted range, and the queued
+// node pairs are summed after the walk -- before, if the queue fills up.
+// The regions and the pairs are those of walk(); the force is summed in
+// another order: the far regions in walk order, then the pairs in walk order.
+constexpr int DEFER_QUEUE = 16;
+
+template <class R, bool ADJUST>
+__device__ __forceinline__ void sum_pairs(int k, const int *q, int nq, R xi, R yi, R mi, R si,
+                                          R scaling, const typename RT<R>::R4 *psort, R &ax,
+                                          R &ay)
+{
+    for (int b = 0; b < nq; b++) {
+        const int last = bucket_last(q[b]);
+        for (int j = bucket_first(q[b]); j <= last; j++) {
+            if (j == k) continue;
+            const typename RT<R>::R4 p = psort[j];
+            const R xd = xi - p.x, yd = yi - p.y;
+            const R g = rep_factor<R, ADJUST>(xd * xd + yd * yd, mi * p.z, si + p.w, scaling);
+            ax += xd * g;
+            ay += yd * g;
+        }
+    }
+}
+
+template <class R, bool ADJUST>
+__device__ __forceinline__ typename RT<R>::R2
+walk_deferred(int k, int n, R scaling, R theta2, double theta2d,
+              const typename RT<R>::R4 *psort, const typename RT<R>::R4 *rec_c,
+              const int2 *rec_t, const Agg<R> *agg, const int *rope, int *status)
+{
+    typedef typename RT<R>::R4 R4;
+    const R4 me = psort[k];
+    const R xi = me.x, yi = me.y, mi = me.z, si = me.w;
+    R ax = R(0), ay = R(0);
+    const int nl = n - 1;
+    const unsigned nend = (unsigned) (nl + n);
+    int q[DEFER_QUEUE];
+    int nq = 0;
+    int cur = 0;
+    // one step per region (n - 1) and per single node reached as a leaf (n)
+    const int cap = 2 * n + 64;
+    for (int step = 0; cur != -1; step++) {
+        if ((unsigned) cur >= nend || step > cap) {
+            atomicOr(status + ST_ERROR, ERR_BOUNDS);
+            break;
+        }
+        int bucket;
+        if (cur >= nl) { // a single node
+            const int j = cur - nl;
+            bucket = bucket_pack(j, j);
+            cur = rope[j];
+        } else {
+            const R4 c = rec_c[cur];
+            const int2 t = rec_t[cur];
+            const R xd = xi - c.x, yd = yi - c.y;
+            const R d2 = xd * xd + yd * yd;
+            const R lhs = d2 * theta2;
+            bool far = lhs > c.w;
+            if (sizeof(R) == 4 && fabs_r(lhs - c.w) <= R(DECIDE_BAND) * c.w)
+                far = far_dd(agg + cur, (float) xi, (float) yi, theta2d);
+            if (far) {
+                const R g = fdiv(scaling * (mi * c.z), d2);
+                ax += xd * g;
+                ay += yd * g;
+                cur = t.y;
+                continue;
+            }
+            if (t.x >= 0) {
+                cur = t.x;
+                continue;
+            }
+            if (bucket_last(t.x) >= n) {
+                atomicOr(status + ST_ERROR, ERR_BOUNDS);
+                break;
+            }
+            bucket = t.x;
+            cur = t.y;
+        }
+        if (nq == DEFER_QUEUE) {
+            sum_pairs<R, ADJUST>(k, q, nq, xi, yi, mi, si, scaling, psort, ax, ay);
+            nq = 0;
+        }
+        q[nq++] = bucket;
+    }
+    sum_pairs<R, ADJUST>(k, q, nq, xi, yi, mi, si, scaling, psort, ax, ay);
+    return mk2<R>(ax, ay);
+}
+
+template <class R, bool ADJUST, int MINB>
+__global__ void __launch_bounds__(256, MINB)
+k_traverse_deferred(int n, R scaling, R theta2, double theta2d,
+                    const typename RT<R>::R4 *__restrict__ psort,
+                    const typename RT<R>::R4 *__restrict__ rec_c, const int2 *__restrict__ rec_t,
+                    const Agg<R> *__restrict__ agg, const int *__restrict__ rope,
+                    const uint32_t *__restrict__ order, typename RT<R>::R2 *__restrict__ f,
+                    int *__restrict__ status)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    f[order[k]] = walk_deferred<R, ADJUST>(k, n, scaling, theta2, theta2d, psort, rec_c, rec_t,
+                                           agg, rope, status);
+}
+
 // The walk of P sorted nodes k0 .. k0+cnt-1 (cnt <= P, neighbours in
 // Morton order) by one thread. The thread walks the union of the nodes'
 // walks, in the same preorder, loading each region once for all of them.
@@ -951,10 +1058,18 @@ k_traverse_count(int n, R theta2, double theta2d, const typename RT<R>::R4 *__re
 
 // ---- 6. gravity and attraction (pipeline.cl:389-429) -----------------------
 
+// Nodes of at least this many incidences (hubs of scale-free graphs) are
+// summed by a warp each in the FP32 path (k_attract_heavy, launched before
+// the attraction): one thread looping over a hub's thousands of incidences
+// would hold up its whole launch. The FP64 path keeps one thread per node:
+// its sums follow the reference's edge order.
+constexpr int HEAVY_DEGREE = 128;
+
 // Gravity and attraction on node i of a graph whose arrays start at pos,
 // mass, size (node indices of inc are relative to them), added to the
-// repulsion already in f[i].
-template <class R>
+// repulsion already in f[i]. SKIP_HEAVY: a node of HEAVY_DEGREE incidences
+// or more gets its gravity only (k_attract_heavy added its attraction).
+template <class R, bool SKIP_HEAVY = false>
 __device__ __forceinline__ void attract_one(int i, R gravity, int strong, int linlog, int adjust,
                                             const typename RT<R>::R2 *pos,
                                             const R *mass,
@@ -965,7 +1080,7 @@ __device__ __forceinline__ void attract_one(int i, R gravity, int strong, int li
 {
     const typename RT<R>::R2 p = pos[i];
     const R xi = p.x, yi = p.y;
-    typename RT<R>::R2 a = f[i];
+    const typename RT<R>::R2 a = f[i];
     R ax = a.x, ay = a.y;
     if (gravity != R(0)) {
         const R dist = fsqrt(xi * xi + yi * yi);
@@ -977,6 +1092,10 @@ __device__ __forceinline__ void attract_one(int i, R gravity, int strong, int li
     }
     const R si = adjust ? size[i] : R(0);
     const int e1 = off[i + 1];
+    if (SKIP_HEAVY && e1 - off[i] >= HEAVY_DEGREE) {
+        f[i] = mk2<R>(ax, ay);
+        return;
+    }
     // incidences in edge order; the loads of four are issued before any of
     // their neighbours' positions is needed (memory-level parallelism), and
     // the sum keeps the order
@@ -1014,7 +1133,65 @@ k_attract(int n, R gravity, int strong, int linlog, int adjust,
           const Inc<R> *__restrict__ inc, typename RT<R>::R2 *__restrict__ f)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) attract_one<R>(i, gravity, strong, linlog, adjust, pos, mass, size, off, inc, f);
+    if (i < n)
+        attract_one<R, sizeof(R) == 4>(i, gravity, strong, linlog, adjust, pos, mass, size, off,
+                                       inc, f);
+}
+
+// The nodes of HEAVY_DEGREE incidences or more (any order: each is summed
+// on its own). `list` holds room for ninc / HEAVY_DEGREE of them, and its
+// count after them.
+static __global__ void __launch_bounds__(256)
+k_heavy_list(int n, const int *__restrict__ off, int *__restrict__ list, int cap)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n || off[i + 1] - off[i] < HEAVY_DEGREE) return;
+    const int k = atomicAdd(list + cap, 1);
+    if (k < cap) list[k] = i;
+}
+
+// The attraction of the heavy nodes (FP32 path), one warp per node, added to
+// the repulsion in f: lane l sums incidences l, l + 32, ... in order, then
+// the lanes' sums are added pairwise across lane distances 16, 8, 4, 2, 1
+// (every lane ends with the same total). Gravity follows in the attraction
+// launch.
+template <class R>
+__global__ void __launch_bounds__(256)
+k_attract_heavy(int nheavy, const int *__restrict__ list, int linlog, int adjust,
+                const typename RT<R>::R2 *__restrict__ pos, const R *__restrict__ size,
+                const int *__restrict__ off, const Inc<R> *__restrict__ inc,
+                typename RT<R>::R2 *__restrict__ f)
+{
+    const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (w >= nheavy) return; // the whole warp
+    const int i = list[w];
+    const typename RT<R>::R2 p = pos[i];
+    const R xi = p.x, yi = p.y;
+    const R si = adjust ? size[i] : R(0);
+    const int e1 = off[i + 1];
+    R ax = R(0), ay = R(0);
+    for (int e = off[i] + lane; e < e1; e += 32) {
+        const Inc<R> c = inc[e];
+        const typename RT<R>::R2 q = pos[c.j];
+        const R xd = xi - q.x, yd = yi - q.y;
+        R g = -c.coef;
+        if (adjust || linlog) {
+            R dist = fsqrt(xd * xd + yd * yd);
+            if (adjust) dist -= si + size[c.j];
+            if (!(dist > R(0))) continue;
+            if (linlog) g *= fdiv(flog1p(dist), dist);
+        }
+        ax += xd * g;
+        ay += yd * g;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        ax += __shfl_xor_sync(0xffffffffu, ax, o);
+        ay += __shfl_xor_sync(0xffffffffu, ay, o);
+    }
+    if (lane == 0) {
+        const typename RT<R>::R2 a = f[i];
+        f[i] = mk2<R>(a.x + ax, a.y + ay);
+    }
 }
 
 // ---- 7. swinging, traction, FP64 totals and the speed update --------------
@@ -1116,20 +1293,22 @@ __device__ __forceinline__ ff2 ff_shfl_down(ff2 a, int o)
     return ff2{__shfl_down_sync(0xffffffffu, a.hi, o), __shfl_down_sync(0xffffffffu, a.lo, o)};
 }
 
-// The end of the totals, by every thread of every block of the kernel: each
-// warp's sums (float-float in the FP32 path, whose 48 bits hold the sum of
-// 32 floats to ~1e-14; double in the FP64 path), then in double from there
-// on: the warps' sums by thread 0 with Neumaier compensation into a partial
-// per block, then the last block to finish sums the partials with Neumaier
+// The end of the totals, by every thread of every block of the kernel. Each
+// block sums its nodes' values in a fixed tree order -- float-float in the
+// FP32 path (FP32 operations only: FP64 instructions cost ~64 cycles of
+// latency a step on a GB300), double in the FP64 path -- into a partial that
+// is exact in double (a float-float pair (hi, lo) is the double hi + lo).
+// The last block to finish sums the partials in double with Neumaier
 // compensation, in a fixed order -- or, up to SERIAL_TOTALS_MAX nodes in the
-// FP64 path, sums the nodes serially in node order (the reference's order)
-// -- and updates Gephi's adaptive speed in double.
+// FP64 path, the nodes serially in node order (the reference's order) -- and
+// updates Gephi's adaptive speed in double.
 template <class R>
 __device__ __forceinline__ void swing_finish(SwingAcc<R> acc, int n, const uint8_t *fixed,
                                              const R *sw, const R *tr, double2 *partial,
                                              unsigned *ticket, SpeedState *st, int *status)
 {
     __shared__ double ss[32], st_[32];
+    __shared__ ff2 fss[32], fst[32];
     __shared__ int last;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
     if constexpr (sizeof(R) == 4) {
@@ -1137,9 +1316,9 @@ __device__ __forceinline__ void swing_finish(SwingAcc<R> acc, int n, const uint8
             acc.s = ff_add(acc.s, ff_shfl_down(acc.s, o));
             acc.t = ff_add(acc.t, ff_shfl_down(acc.t, o));
         }
-        if (lane == 0) { // hi + lo is exact in double
-            ss[w] = ff_to_double(acc.s);
-            st_[w] = ff_to_double(acc.t);
+        if (lane == 0) {
+            fss[w] = acc.s;
+            fst[w] = acc.t;
         }
     } else {
         acc.ds = warp_sum(acc.ds);
@@ -1151,12 +1330,22 @@ __device__ __forceinline__ void swing_finish(SwingAcc<R> acc, int n, const uint8
     }
     __syncthreads();
     if (threadIdx.x == 0) {
-        double a = 0.0, b = 0.0, ca = 0.0, cb = 0.0;
-        for (int k = 0; k < nw; k++) {
-            neumaier(a, ca, ss[k]);
-            neumaier(b, cb, st_[k]);
+        if constexpr (sizeof(R) == 4) {
+            ff2 a = fss[0], b = fst[0];
+            for (int k = 1; k < nw; k++) {
+                a = ff_add(a, fss[k]);
+                b = ff_add(b, fst[k]);
+            }
+            // (hi, lo) of both sums: the exact doubles a.hi + a.lo, b.hi + b.lo
+            reinterpret_cast<float4 *>(partial)[blockIdx.x] = make_float4(a.hi, a.lo, b.hi, b.lo);
+        } else {
+            double a = 0.0, b = 0.0, ca = 0.0, cb = 0.0;
+            for (int k = 0; k < nw; k++) {
+                neumaier(a, ca, ss[k]);
+                neumaier(b, cb, st_[k]);
+            }
+            partial[blockIdx.x] = make_double2(__dadd_rn(a, ca), __dadd_rn(b, cb));
         }
-        partial[blockIdx.x] = make_double2(__dadd_rn(a, ca), __dadd_rn(b, cb));
         __threadfence();
         last = atomicAdd(ticket, 1u) == gridDim.x - 1;
     }
@@ -1187,7 +1376,14 @@ __device__ __forceinline__ void swing_finish(SwingAcc<R> acc, int n, const uint8
     } else {
         double s1 = 0.0, c1 = 0.0, s2 = 0.0, c2 = 0.0;
         for (int k = threadIdx.x; k < (int) gridDim.x; k += blockDim.x) {
-            const double2 v = __ldcg(partial + k);
+            double2 v;
+            if constexpr (sizeof(R) == 4) {
+                const float4 q = __ldcg(reinterpret_cast<const float4 *>(partial) + k);
+                v = make_double2(__dadd_rn((double) q.x, (double) q.y),
+                                 __dadd_rn((double) q.z, (double) q.w));
+            } else {
+                v = __ldcg(partial + k);
+            }
             neumaier(s1, c1, v.x);
             neumaier(s2, c2, v.y);
         }
@@ -1237,7 +1433,8 @@ k_attract_swing(int n, R gravity, int strong, int linlog, int adjust,
     SwingAcc<R> acc;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) {
-        attract_one<R>(i, gravity, strong, linlog, adjust, pos, mass, size, off, inc, f);
+        attract_one<R, sizeof(R) == 4>(i, gravity, strong, linlog, adjust, pos, mass, size, off,
+                                       inc, f);
         swing_node<R>(i, n, f, fold, mass, fixed, sw, tr, acc);
     }
     swing_finish<R>(acc, n, fixed, sw, tr, partial, ticket, st, status);

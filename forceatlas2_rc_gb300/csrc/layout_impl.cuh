@@ -103,6 +103,11 @@ template <class R> struct Layout : LayoutBase {
     uint8_t *fixed = nullptr;
     int *inc_off = nullptr;
     Inc<R> *inc = nullptr;
+    // FP32: the nodes of HEAVY_DEGREE incidences or more (heavy_cap of room,
+    // then their count), summed by a warp each
+    int *heavy = nullptr;
+    int heavy_cap = 0, nheavy = 0;
+    int launches = 0; // kernels of one captured iteration
     R *bbox = nullptr, *bbox_partial = nullptr;
     double *quant = nullptr; // min x, min y, Morton scale, -, 4 floats (k_bbox)
     int nbbox = 1;
@@ -151,6 +156,10 @@ template <class R> struct Layout : LayoutBase {
         fixed = any_fixed ? mem.get<uint8_t>(nn) : nullptr;
         inc_off = mem.get<int>(nn + 1);
         inc = mem.get<Inc<R>>((size_t) ninc);
+        if (sizeof(R) == 4) {
+            heavy_cap = ninc / HEAVY_DEGREE;
+            heavy = mem.get<int>((size_t) heavy_cap + 1);
+        }
         swing_partial = mem.get<double2>((size_t) ceil_div(n, 256)); // one per block
         st = mem.get<SpeedState>(1);
         status = mem.get<int>(ST_COUNT);
@@ -274,6 +283,7 @@ template <class R> struct Layout : LayoutBase {
             FA2_TRY(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking),
                     "could not create a CUDA stream", 1);
         for (auto &e : ev) FA2_TRY(cudaEventCreate(&e), "could not create a CUDA event", 1);
+
         mem.pool = opts ? opts->pool : nullptr;
         mem.s = s;
         if (rep == FA2CU_REPULSION_BH && sort_setup()) return 1;
@@ -337,6 +347,17 @@ template <class R> struct Layout : LayoutBase {
                 set_cuda_error("could not send the graph to the device", cudaGetLastError());
                 return 1;
             }
+        }
+        // the heavy nodes (FP32), listed once
+        if (heavy) {
+            FA2_TRY(cudaMemsetAsync(heavy + heavy_cap, 0, sizeof(int), s), "cudaMemset", 1);
+            if (heavy_cap > 0)
+                k_heavy_list<<<ceil_div(n, 256), 256, 0, s>>>(n, inc_off, heavy, heavy_cap);
+            FA2_TRY(cudaMemcpyAsync(&nheavy, heavy + heavy_cap, sizeof(int),
+                                    cudaMemcpyDeviceToHost, s),
+                    "could not prepare the layout", 1);
+            FA2_TRY(cudaStreamSynchronize(s), "could not prepare the layout", 1);
+            nheavy = std::min(nheavy, heavy_cap);
         }
         // status words (error flags, arrival tickets) and the previous
         // forces start at zero; then the positions (and their bounding box,
@@ -451,6 +472,15 @@ template <class R> struct Layout : LayoutBase {
                         <<<ceil_div(n, 256), 256, 0, s>>>(n, scaling, theta2, theta2d, psort,
                                                           rec_c, rec_t, agg, rope, order, f,
                                                           status);
+            } else if (walk == WALK_DEFERRED) {
+                if (adjust)
+                    k_traverse_deferred<R, true, 6><<<ceil_div(n, 256), 256, 0, s>>>(
+                        n, scaling, theta2, theta2d, psort, rec_c, rec_t, agg, rope, order, f, status);
+                else
+                    k_traverse_deferred<R, false, sizeof(R) == 4 ? 8 : 6>
+                        <<<ceil_div(n, 256), 256, 0, s>>>(n, scaling, theta2, theta2d, psort,
+                                                          rec_c, rec_t, agg, rope, order, f,
+                                                          status);
             } else if (walk == WALK_PAIR) {
                 const int grid = ceil_div(ceil_div(n, 2), 256);
                 if (adjust)
@@ -481,9 +511,17 @@ template <class R> struct Layout : LayoutBase {
                                        status);
         }
     }
+    // The heavy nodes' attraction (FP32), added to their repulsion.
+    void launch_heavy()
+    {
+        if (nheavy > 0)
+            k_attract_heavy<R><<<ceil_div(nheavy, 8), 256, 0, s>>>(nheavy, heavy, linlog, adjust,
+                                                                  pos, size, inc_off, inc, f);
+    }
     // Attraction and gravity only (the forces of fa2cu_layout_forces).
     void launch_attraction()
     {
+        launch_heavy();
         k_attract<R><<<ceil_div(n, 256), 256, 0, s>>>(n, gravity, strong, linlog, adjust, pos,
                                                       mass, size, inc_off, inc, f);
     }
@@ -493,6 +531,7 @@ template <class R> struct Layout : LayoutBase {
     {
         // serial totals: the last block stages 2n reals
         const size_t smem = serial_totals<R>(n) ? 2 * (size_t) n * sizeof(R) : 0;
+        launch_heavy();
         k_attract_swing<R><<<ceil_div(n, 256), 256, smem, s>>>(
             n, gravity, strong, linlog, adjust, pos, mass, size, inc_off, inc, f, fold, fixed, sw,
             trac, swing_partial, (unsigned *) (status + ST_TICKET_SWING), st, status);
@@ -538,6 +577,20 @@ template <class R> struct Layout : LayoutBase {
         if (e != cudaSuccess) {
             set_cuda_error("could not capture the iteration", e);
             return 1;
+        }
+        if (iters == 1) { // the kernels of one iteration
+            size_t nodes = 0;
+            if (cudaGraphGetNodes(g, nullptr, &nodes) == cudaSuccess) {
+                std::vector<cudaGraphNode_t> v(nodes);
+                launches = 0;
+                if (nodes && cudaGraphGetNodes(g, v.data(), &nodes) == cudaSuccess)
+                    for (cudaGraphNode_t x : v) {
+                        cudaGraphNodeType t;
+                        if (cudaGraphNodeGetType(x, &t) == cudaSuccess &&
+                            t == cudaGraphNodeTypeKernel)
+                            launches++;
+                    }
+            }
         }
         e = cudaGraphInstantiate(out, g, 0);
         cudaGraphDestroy(g);
@@ -730,7 +783,7 @@ template <class R> struct Layout : LayoutBase {
         }
         if (!strcmp(name, "walk") &&
             (value == WALK_WARP || value == WALK_THREAD || value == WALK_THREAD_WIDE ||
-             value == WALK_PAIR || value == WALK_QUAD)) {
+             value == WALK_PAIR || value == WALK_QUAD || value == WALK_DEFERRED)) {
             walk = (int) value;
             return recapture();
         }
@@ -750,6 +803,16 @@ template <class R> struct Layout : LayoutBase {
         }
         set_message("unknown option %s = %g", name, value);
         return 1;
+    }
+
+    double info(const char *name) override
+    {
+        if (!strcmp(name, "launches_per_iteration")) return launches;
+        if (!strcmp(name, "heavy_nodes")) return nheavy;
+        if (!strcmp(name, "nodes")) return n;
+        if (!strcmp(name, "incidences")) return ninc;
+        set_message("unknown layout information %s", name);
+        return -1.0;
     }
 
     int swing(double *hsw, double *htr) override

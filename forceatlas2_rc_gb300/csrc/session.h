@@ -27,6 +27,7 @@ struct LayoutBase {
     virtual int traversal_counts(double counts[2]) = 0;
     virtual int option(const char *name, double value) = 0;
     virtual int swing(double *sw, double *tr) = 0;
+    virtual double info(const char *name) = 0;
     virtual double bytes() const = 0;
     int device = 0;
 };

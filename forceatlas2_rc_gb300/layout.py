@@ -300,6 +300,14 @@ class Layout:
         self._check(self.lib.fa2cu_layout_traversal_counts(self.h, dptr(c)))
         return dict(visits=c[0], pairs=c[1])
 
+    def info(self, name: str) -> float:
+        """fa2cu_layout_info: "launches_per_iteration", "heavy_nodes",
+        "nodes", "incidences"."""
+        v = self.lib.fa2cu_layout_info(self.h, name.encode())
+        if v < 0:
+            raise RuntimeError(_lib.error())
+        return v
+
     def swing(self, traction: bool = False):
         """Per-node swinging (and traction, after option("keep_traction",
         1)) of the last iteration."""

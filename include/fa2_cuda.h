@@ -94,6 +94,12 @@ int fa2cu_layout_traversal_counts(fa2cu_layout *L, double counts[2]);
  *                  fa2cu_layout_swing (n more reals on the device). */
 int fa2cu_layout_option(fa2cu_layout *L, const char *name, double value);
 
+/* A figure of the layout, by name: "launches_per_iteration" (kernels of one
+ * captured iteration), "heavy_nodes" (nodes of 128 incidences or more, whose
+ * attraction a warp each sums in single precision), "nodes", "incidences".
+ * -1 with a message for an unknown name. */
+double fa2cu_layout_info(fa2cu_layout *L, const char *name);
+
 /* Each node's swinging (sw, n doubles) and traction (tr, n doubles; needs
  * the option keep_traction, else pass NULL) of the last iteration, the
  * values the swing/traction totals of fa2cu_layout_speed sum (fixed nodes

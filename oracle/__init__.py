@@ -22,7 +22,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "_build", "libfa2oracle.so")
 REF_LIB = os.path.join(HERE, "_ref", "libfa2ref.so")
 REF_CUDA_LIB = os.path.join(HERE, "_ref", "libfa2ref_cuda.so")
-REF_SRC = "/root/reference"
+# the reference checkout (where present): FA2_REF in the environment, else
+# where this container keeps it; the GPU host has none
+REF_SRC = os.environ.get("FA2_REF") or "/root/reference"
 
 
 def build(ref: bool = False, quiet: bool = True) -> None:
@@ -31,7 +33,7 @@ def build(ref: bool = False, quiet: bool = True) -> None:
     out = subprocess.DEVNULL if quiet else None
     subprocess.run(["make", "-C", HERE, "-s"], check=True, stdout=out)
     if ref and os.path.isdir(os.path.join(REF_SRC, "src")):
-        subprocess.run(["make", "-C", HERE, "-s", "ref"], check=True,
+        subprocess.run(["make", "-C", HERE, "-s", "ref", f"REF={REF_SRC}"], check=True,
                        stdout=out)
 
 

@@ -856,11 +856,85 @@ static void repulse_mixed(const pipe_ws_f *w, const pipe_ws_d *wd,
     }
 }
 
+/* Its attraction: as attract_core_f, except that a node of at least
+ * ORC_HEAVY incidences gets its attraction first, as 32 interleaved partial
+ * sums (incidence e to partial e mod 32, each in edge order) added pairwise
+ * across distances 16, 8, 4, 2, 1 -- a warp's sum on the device -- then its
+ * gravity. */
+#define ORC_HEAVY 128
+static void attract_mixed(int n, float gravity, int strong, int linlog,
+                          int adjust, const float *p, const float *mass,
+                          const float *size, const int *off,
+                          const int *inc_node, const float *inc_coef, float *f)
+{
+    for (int i = 0; i < n; i++) {
+        const float xi = p[2 * i], yi = p[2 * i + 1];
+        const float si = adjust ? size[i] : 0.0f;
+        const int heavy = off[i + 1] - off[i] >= ORC_HEAVY;
+        if (heavy) {
+            float lx[32], ly[32];
+            for (int l = 0; l < 32; l++) {
+                lx[l] = ly[l] = 0.0f;
+                for (int e = off[i] + l; e < off[i + 1]; e += 32) {
+                    const int j = inc_node[e];
+                    const float xd = xi - p[2 * j], yd = yi - p[2 * j + 1];
+                    float g = -inc_coef[e];
+                    if (adjust || linlog) {
+                        float dist = sqrtf(xd * xd + yd * yd);
+                        if (adjust) dist -= si + size[j];
+                        if (!(dist > 0.0f)) continue;
+                        if (linlog) g *= log1pf(dist) / dist;
+                    }
+                    lx[l] += xd * g;
+                    ly[l] += yd * g;
+                }
+            }
+            for (int o = 16; o > 0; o >>= 1) {
+                float tx[32], ty[32];
+                for (int l = 0; l < 32; l++) {
+                    tx[l] = lx[l] + lx[l ^ o];
+                    ty[l] = ly[l] + ly[l ^ o];
+                }
+                memcpy(lx, tx, sizeof(lx));
+                memcpy(ly, ty, sizeof(ly));
+            }
+            f[2 * i] += lx[0];
+            f[2 * i + 1] += ly[0];
+        }
+        float ax = f[2 * i], ay = f[2 * i + 1];
+        if (gravity != 0.0f) {
+            const float dist = sqrtf(xi * xi + yi * yi);
+            if (dist > 0.0f) {
+                const float g = strong ? gravity * mass[i] : gravity * mass[i] / dist;
+                ax -= xi * g;
+                ay -= yi * g;
+            }
+        }
+        if (!heavy) {
+            for (int e = off[i]; e < off[i + 1]; e++) {
+                const int j = inc_node[e];
+                const float xd = xi - p[2 * j], yd = yi - p[2 * j + 1];
+                float g = -inc_coef[e];
+                if (adjust || linlog) {
+                    float dist = sqrtf(xd * xd + yd * yd);
+                    if (adjust) dist -= si + size[j];
+                    if (!(dist > 0.0f)) continue;
+                    if (linlog) g *= log1pf(dist) / dist;
+                }
+                ax += xd * g;
+                ay += yd * g;
+            }
+        }
+        f[2 * i] = ax;
+        f[2 * i + 1] = ay;
+    }
+}
+
 /* Forces as that path computes them: the tree is built in double from the
  * positions and masses rounded to float (keys, order, regions: the double
  * construction of pipeline.cl), the regions' records are rounded to float,
- * and the walk (with the decisions above) and the attraction run in float
- * (pipeline.cl:332-429). */
+ * and the walk (with the decisions above) and the attraction (with the
+ * heavy nodes' order above) run in float (pipeline.cl:332-429). */
 int orc_pipe_forces_m(const fa2_full_params *pp, const double *pos,
                       double *fout)
 {
@@ -900,9 +974,9 @@ int orc_pipe_forces_m(const fa2_full_params *pp, const double *pos,
         repulse_mixed(&wf, &wd, (float) pp->scaling,
                       (float) (pp->theta * pp->theta), pp->theta * pp->theta,
                       pp->adjust, f);
-        attract_core_f(n, (float) pp->gravity, pp->strong, pp->linlog,
-                       pp->adjust, gf.p, gf.mass, gf.size, pp->inc_off,
-                       pp->inc_node, gf.coef, f);
+        attract_mixed(n, (float) pp->gravity, pp->strong, pp->linlog,
+                      pp->adjust, gf.p, gf.mass, gf.size, pp->inc_off,
+                      pp->inc_node, gf.coef, f);
         for (int i = 0; i < n; i++) {
             fout[i] = (double) f[2 * i];
             fout[n + i] = (double) f[2 * i + 1];

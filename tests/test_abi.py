@@ -88,7 +88,8 @@ def test_reference_driver_links_against_backend(cuda_lib):
     import oracle
     if not os.path.isdir(os.path.join(oracle.REF_SRC, "src")):
         pytest.skip("reference checkout not present")
-    subprocess.run(["make", "-C", oracle.HERE, "-s", "ref-cuda"], check=True)
+    subprocess.run(["make", "-C", oracle.HERE, "-s", "ref-cuda", f"REF={oracle.REF_SRC}"],
+                   check=True)
     lib = C.CDLL(oracle.REF_CUDA_LIB)
     lib.ref_error.restype = C.c_char_p
     n = 10

@@ -427,3 +427,35 @@ def test_config2_ba100k_forces(gpu, orc):
     assert rel_err(ff, orc.pipe_forces(p, pos, "m")) <= 1e-5
     # and after 20 iterations of the FP32 layout, from its own positions
     assert rel_err(ff2, orc.pipe_forces(p, xy, "d")) <= 1e-4
+
+
+@pytest.mark.parametrize("opts", [dict(), dict(linlog=True), dict(adjust=True, linlog=True)])
+def test_heavy_nodes_single(gpu, orc, opts):
+    """FP32: nodes of 128 incidences or more (hubs) have their attraction
+    summed by a warp each, in a fixed order that the oracle's restatement of
+    the FP32 path mirrors: forces within 1e-5 of it, and within 1e-4 of the
+    FP64 forces (2e-3 with prevent_overlap); the hub kernel is one more
+    launch per iteration."""
+    n, a, b = G.barabasi_albert(6000, 3, seed=12)
+    rng = np.random.default_rng(13)
+    hub_a = np.concatenate([np.zeros(3000, np.int32), np.ones(700, np.int32)])
+    hub_b = np.concatenate([rng.choice(np.arange(2, n), 3000, replace=False),
+                            rng.choice(np.arange(2, n), 700, replace=False)]).astype(np.int32)
+    a, b = np.concatenate([a, hub_a]), np.concatenate([b, hub_b])
+    w = rng.lognormal(0.0, 0.5, len(a))
+    pos = f32(G.uniform_positions(n, 0, 1000, seed=14))
+    size = f32(rng.uniform(0.5, 3.0, n)) if opts.get("adjust") else None
+    go = orc.prepare_large(n, a, b, w)
+    p, keep = orc.full_params(go, size=size, theta=1.2, **opts)
+    with make_layout(n, a, b, w, pos, "single", size=size, theta=1.2, **opts) as L:
+        f = L.forces(pos)
+        heavy = L.info("heavy_nodes")
+        launches = L.info("launches_per_iteration")
+    with make_layout(n, a, b, w, pos, "double", size=size, theta=1.2, **opts) as L:
+        fd = L.forces(pos)
+        launches_d = L.info("launches_per_iteration")
+    deg = np.diff(go.inc_off)
+    assert heavy == (deg >= 128).sum() > 2
+    assert launches == launches_d + 1
+    assert rel_err(f, orc.pipe_forces(p, pos, "m")) <= 1e-5
+    assert rel_err(f, fd) <= (2e-3 if opts.get("adjust") else 1e-4)
