@@ -1295,13 +1295,15 @@ __device__ __forceinline__ ff2 ff_shfl_down(ff2 a, int o)
 
 // The end of the totals, by every thread of every block of the kernel. Each
 // block sums its nodes' values in a fixed tree order -- float-float in the
-// FP32 path (FP32 operations only: FP64 instructions cost ~64 cycles of
-// latency a step on a GB300), double in the FP64 path -- into a partial that
-// is exact in double (a float-float pair (hi, lo) is the double hi + lo).
-// The last block to finish sums the partials in double with Neumaier
-// compensation, in a fixed order -- or, up to SERIAL_TOTALS_MAX nodes in the
-// FP64 path, the nodes serially in node order (the reference's order) -- and
-// updates Gephi's adaptive speed in double.
+// FP32 path (FP32 operations only: a dependent FP64 add costs ~64 cycles on
+// a GB300, and an SM's FP64 pipe completes 2 lanes a cycle), double in the
+// FP64 path -- into a partial (a float-float pair (hi, lo) is the exact
+// double hi + lo). The last block to finish sums the partials in a fixed
+// order: in the FP64 path with Neumaier compensation in double; in the FP32
+// path in float-float, then the warps' sums in double with Neumaier
+// compensation -- or, up to SERIAL_TOTALS_MAX nodes in the FP64 path, the
+// nodes serially in node order (the reference's order) -- and updates
+// Gephi's adaptive speed in double.
 template <class R>
 __device__ __forceinline__ void swing_finish(SwingAcc<R> acc, int n, const uint8_t *fixed,
                                              const R *sw, const R *tr, double2 *partial,
@@ -1373,17 +1375,42 @@ __device__ __forceinline__ void swing_finish(SwingAcc<R> acc, int n, const uint8
                 ttr = __dadd_rn(ttr, (double) str[i]);
             }
         }
+    } else if constexpr (sizeof(R) == 4) {
+        // the partials per thread (strided, fixed order) and per warp in
+        // float-float, whose same-sign sums lose about 2^-47 relative a step
+        // (FP32 instructions: this block runs on one SM, whose FP64 pipe
+        // completes 2 lanes a cycle); then the warps' sums in FP64 with
+        // Neumaier compensation
+        ff2 a = ff2{0.0f, 0.0f}, b = ff2{0.0f, 0.0f};
+        const float4 *pf = reinterpret_cast<const float4 *>(partial);
+        for (int k = threadIdx.x; k < (int) gridDim.x; k += blockDim.x) {
+            const float4 v = __ldcg(pf + k);
+            a = ff_add(a, ff2{v.x, v.y});
+            b = ff_add(b, ff2{v.z, v.w});
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            a = ff_add(a, ff_shfl_down(a, o));
+            b = ff_add(b, ff_shfl_down(b, o));
+        }
+        __syncthreads();
+        if (lane == 0) { // hi + lo is exact in double
+            ss[w] = ff_to_double(a);
+            st_[w] = ff_to_double(b);
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double t1 = 0.0, k1 = 0.0, t2 = 0.0, k2 = 0.0;
+            for (int k = 0; k < nw; k++) {
+                neumaier(t1, k1, ss[k]);
+                neumaier(t2, k2, st_[k]);
+            }
+            tsw = __dadd_rn(t1, k1);
+            ttr = __dadd_rn(t2, k2);
+        }
     } else {
         double s1 = 0.0, c1 = 0.0, s2 = 0.0, c2 = 0.0;
         for (int k = threadIdx.x; k < (int) gridDim.x; k += blockDim.x) {
-            double2 v;
-            if constexpr (sizeof(R) == 4) {
-                const float4 q = __ldcg(reinterpret_cast<const float4 *>(partial) + k);
-                v = make_double2(__dadd_rn((double) q.x, (double) q.y),
-                                 __dadd_rn((double) q.z, (double) q.w));
-            } else {
-                v = __ldcg(partial + k);
-            }
+            const double2 v = __ldcg(partial + k);
             neumaier(s1, c1, v.x);
             neumaier(s2, c2, v.y);
         }

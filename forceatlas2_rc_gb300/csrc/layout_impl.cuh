@@ -66,7 +66,10 @@ template <class R> struct Layout : LayoutBase {
 
     int n = 0, ninc = 0, repulsion = 0, adjust = 0, strong = 0, linlog = 0;
     int any_fixed = 0;
-    int walk = WALK_THREAD;
+    // FP32: the walk with deferred node pairs (0.48-0.52 against 0.57-0.61
+    // ms at 10^6 nodes); FP64: one walk per thread, in the reference's
+    // order of the forces
+    int walk = sizeof(R) == 4 ? WALK_DEFERRED : WALK_THREAD;
     int climb_mode = 1; // leaves per aggregate thread (negative: interleaved)
     bool block_sort = false; // few keys: the one-block sort
 

@@ -75,13 +75,18 @@ int fa2cu_layout_tree(fa2cu_layout *L, const double *pos, uint32_t *key,
  * the current positions (an instrumented, untimed variant). */
 int fa2cu_layout_traversal_counts(fa2cu_layout *L, double counts[2]);
 
-/* Set a tuning option of the layout (every choice gives identical results;
- * nonzero and a message for an unknown name or value):
+/* Set a tuning option of the layout (nonzero and a message for an unknown
+ * name or value). Every walk computes the same interactions; walks 0-4 add
+ * them up in the same order (identical forces), walk 5 in another (forces
+ * equal to ~1e-7 in single precision):
  *   "walk"         Barnes-Hut walk: 1 one independent walk per thread
- *                  (default), 0 warp-synchronous (lanes walk together,
- *                  keeping their own decisions), 2 the per-thread walk
- *                  compiled without its register bound, 3 / 4 two / four
- *                  Morton neighbours per thread;
+ *                  (default in double precision), 0 warp-synchronous (lanes
+ *                  walk together, keeping their own decisions), 2 the
+ *                  per-thread walk compiled without its register bound, 3 /
+ *                  4 two / four Morton neighbours per thread, 5 one walk per
+ *                  thread visiting regions only, its node pairs queued and
+ *                  summed after the far regions (default in single
+ *                  precision);
  *   "climb"        leaves per thread of the bottom-up sums: 1, 2, 4 or 8
  *                  contiguous, -2 or -4 interleaved over the warp (default:
  *                  1 below one wave of threads, else 2 in float, 4 in

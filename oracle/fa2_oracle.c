@@ -798,17 +798,23 @@ void orc_pipe_tree(int n, const uint32_t *key, int *child, int *range,
 /* The float walk of that path: regions in float, but a region whose test
  * d^2 theta^2 > size^2 is within 1e-4 of the boundary is decided in double
  * from the double construction, so that the float path approximates the
- * regions the double path approximates. */
+ * regions the double path approximates. The forces of the far regions are
+ * added in walk order, then those of the node pairs (the small regions too
+ * close and the single nodes), in walk order: the order of the path's walk,
+ * which queues the pairs (walk_deferred). */
 static void repulse_mixed(const pipe_ws_f *w, const pipe_ws_d *wd,
                           float scaling, float theta2, double theta2d,
                           int adjust, float *f)
 {
     const int n = w->n;
     const float *ps = w->psort, *ni = w->ni;
+    int *pairs = (int *) malloc(2 * (size_t) n * 2 * sizeof(int));
+    if (!pairs) return;
     for (int k = 0; k < n; k++) {
         const float xi = ps[4 * k], yi = ps[4 * k + 1];
         const float mi = ps[4 * k + 2], si = ps[4 * k + 3];
         float ax = 0.0f, ay = 0.0f;
+        int np = 0; /* queued ranges (first, last) */
         int stack[160];
         int sp = 0;
         stack[sp++] = 0;
@@ -841,7 +847,12 @@ static void repulse_mixed(const pipe_ws_f *w, const pipe_ws_d *wd,
                     continue;
                 }
             }
-            for (int j = first; j <= last; j++) {
+            pairs[2 * np] = first;
+            pairs[2 * np + 1] = last;
+            np++;
+        }
+        for (int b = 0; b < np; b++) {
+            for (int j = pairs[2 * b]; j <= pairs[2 * b + 1]; j++) {
                 if (j == k) continue;
                 const float xd = xi - ps[4 * j], yd = yi - ps[4 * j + 1];
                 const float g = rep_f(xd * xd + yd * yd, mi * ps[4 * j + 2],
@@ -854,6 +865,7 @@ static void repulse_mixed(const pipe_ws_f *w, const pipe_ws_d *wd,
         f[2 * i] = ax;
         f[2 * i + 1] = ay;
     }
+    free(pairs);
 }
 
 /* Its attraction: as attract_core_f, except that a node of at least
