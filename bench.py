@@ -956,8 +956,7 @@ def headline(args, local, ws, pg):
     g = Graph(n, a, b, np.ones(len(a)), outbound=True)
     kw = dict(scaling=2.0, gravity=1.0, theta=1.2, linlog=True, device=local)
     L = Layout(g, pos, precision="single", repulsion=REPULSION_BH, **kw)
-    if args.walk != "thread":
-        L.option("walk", WALKS[args.walk])
+    L.option("walk", WALKS[args.walk])
     stream = torch.cuda.ExternalStream(L.stream, device=local)
     # kernels of one captured iteration: Morton codes (with the sort's digit
     # histograms), 4 sort passes, gather + Karras tree, the bottom-up sums,
@@ -1137,9 +1136,10 @@ def main():
                          "kernel alone on 100,000 nodes (FP32 pipe figures); "
                          "batch: 4096 graphs in one persistent launch; "
                          "serve: the layout server on a Poisson job trace")
-    ap.add_argument("--walk", default="thread",
+    ap.add_argument("--walk", default="deferred",
                     choices=["warp", "thread", "wide", "pair", "quad", "deferred"],
-                    help="Barnes-Hut walk (identical forces)")
+                    help="Barnes-Hut walk (the same interactions; deferred is the "
+                         "FP32 default)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
