@@ -689,30 +689,17 @@ k_pre_scatter(int n, int adjust, const int2 *__restrict__ child, const int2 *__r
     const int2 rg = range[r];
     const bool open = rg.y - rg.x >= 8;
     if (r != 0 && !open) return;
-    // the records to write: the root (by region 0), and the children of an
-    // open region (regions < nl, single nodes nl + j)
     int xs[3], nx = 0;
-    bool is_leaf[3] = {false, false, false};
-    if (r == 0) xs[nx++] = 0;
+    if (r == 0) xs[nx++] = 0; // the root itself
     if (open) {
         const int2 c = child[r];
-        is_leaf[nx] = c.x >= nl;
         xs[nx++] = c.x;
-        is_leaf[nx] = c.y >= nl;
         xs[nx++] = c.y;
     }
     for (int u = 0; u < nx; u++) {
         const int x = xs[u];
-        const bool leaf = is_leaf[u];
-        if (x < 0 || (leaf ? x - nl >= n : x >= nl)) {
-            atomicOr(status + ST_ERROR, ERR_BOUNDS);
-            continue;
-        }
+        const bool leaf = x >= nl && u > 0; // (the root is a region)
         const int f = leaf ? x - nl : range[x].x;
-        if (f < 0 || f >= n) {
-            atomicOr(status + ST_ERROR, ERR_BOUNDS);
-            continue;
-        }
         const int2 hs = leaf ? make_int2(0, 1) : hsz[x];
         const int pre = bb[f / SPINE_BLOCK] + lpi[f] - 1 - hs.x;
         if (pre < 0 || pre >= P || pre + hs.y > P) {
@@ -1005,14 +992,8 @@ k_traverse_pre(int n, float scaling, float theta2, double theta2d,
         const float lhs = d2 * theta2;
         bool far = lhs > c.w;
         // (a single node's 0 or infinity is never in the band)
-        if (fabsf(lhs - c.w) < DECIDE_BAND * c.w) {
-            const int a = paux[cur];
-            if ((unsigned) a >= (unsigned) (n - 1)) {
-                atomicOr(status + ST_ERROR, ERR_BOUNDS);
-                break;
-            }
-            far = far_dd(agg + a, xi, yi, theta2d);
-        }
+        if (fabsf(lhs - c.w) < DECIDE_BAND * c.w)
+            far = far_dd(agg + paux[cur], xi, yi, theta2d);
         if (far) {
             const float g = fdiv(scaling * (mi * c.z), d2);
             ax += xd * g;
@@ -1025,10 +1006,6 @@ k_traverse_pre(int n, float scaling, float theta2, double theta2d,
             continue;
         }
         const int a = paux[cur];
-        if ((unsigned) a >= (unsigned) ((l & 3) == 2 ? n : n - 1)) {
-            atomicOr(status + ST_ERROR, ERR_BOUNDS);
-            break;
-        }
         int bucket;
         if ((l & 3) == 2) {
             bucket = bucket_pack(a, a);
