@@ -23,13 +23,11 @@ void set_cuda_error(const char *what, cudaError_t e);
         }                                                                      \
     } while (0)
 
-// Barnes-Hut walk variants (all compute the same interactions; 0-4 add them
-// up in the same order): warp-synchronous; one walk per thread at 8 blocks
-// of 256 per SM (<= 32 registers; 6 and <= 40 with prevent_overlap or in
-// double); one walk per thread with the registers the compiler wants; one
-// thread walking for two or four Morton neighbours at once; one walk per
-// thread with its node pairs queued and summed after the walk; the same over
-// the tree re-laid out in preorder (FP32 only).
+// Barnes-Hut walk variants (all give identical forces): warp-synchronous;
+// one walk per thread at 8 blocks of 256 per SM (<= 32 registers; 6 and <= 40
+// with prevent_overlap or in double); one walk
+// per thread with the registers the compiler wants; one thread walking for
+// two or four Morton neighbours at once.
 enum {
     WALK_WARP = 0,
     WALK_THREAD = 1,
@@ -37,7 +35,6 @@ enum {
     WALK_PAIR = 3,
     WALK_QUAD = 4,
     WALK_DEFERRED = 5,
-    WALK_PREORDER = 6,
 };
 
 // Nanoseconds of the GPU's global timer (bounds of every device-side wait).
@@ -69,7 +66,6 @@ enum {
     ST_TICKET_BBOX,    // arrival counters of the last-block reductions
     ST_TICKET_SWING,
     ST_TICKET_NODE,
-    ST_TICKET_SPINE,
     ST_COUNT
 };
 enum {

@@ -485,13 +485,6 @@ template <bool CTA> __device__ __forceinline__ int arrive(int *v)
 
 // The climb of leaf k (sorted position) of an n-node tree: every region it
 // reaches second gets its sums (agg) and its traversal records.
-// With hsz (may be null), it also counts, for the preorder layout of the
-// walk (k_pre_scatter), the regions a walk can visit: hsz[r] = (h, s), s the
-// number of them in r's subtree counting r (1 for a region of at most 8
-// nodes, whose inside is never visited), h the length of r's chain of left
-// children among them; and spine[f] = h + 1 for every right child (and the
-// root) whose range starts at sorted node f: the number of visitable regions
-// and nodes whose range starts at f.
 template <class R, bool CTA>
 __device__ __forceinline__ void climb(int k, int n, const typename RT<R>::R4 *psort,
                                       const int2 *child,
@@ -499,7 +492,7 @@ __device__ __forceinline__ void climb(int k, int n, const typename RT<R>::R4 *ps
                                       const int2 *range,
                                       const int *rope, int *visits,
                                       Agg<R> *agg, typename RT<R>::R4 *rec_c, int2 *rec_t,
-                                      int *status, int2 *hsz = nullptr, int *spine = nullptr)
+                                      int *status)
 {
     const int nl = n - 1;
     int r = parent[nl + k];
@@ -527,19 +520,6 @@ __device__ __forceinline__ void climb(int k, int n, const typename RT<R>::R4 *ps
         agg[r] = q;
         rec_c[r] = agg_record(q);
         rec_t[r] = links;
-        if (hsz) {
-            int2 hr = make_int2(0, 1);
-            if (rg.y - rg.x >= 8) { // a region the walk may open: its children are visitable
-                const int2 ha = c.x >= nl ? make_int2(0, 1) : __ldcg(hsz + c.x);
-                const int2 hb = c.y >= nl ? make_int2(0, 1) : __ldcg(hsz + c.y);
-                hr = make_int2(1 + ha.x, 1 + ha.y + hb.y);
-                // the right child starts at the split + 1, its index as a
-                // leaf or as a region
-                spine[c.y >= nl ? c.y - nl : c.y] = hb.x + 1;
-            }
-            hsz[r] = hr;
-            if (r == 0) spine[0] = hr.x + 1;
-        }
         r = parent[r];
     }
 }
@@ -551,12 +531,12 @@ k_aggregate(int n, const typename RT<R>::R4 *__restrict__ psort,
             const int2 *__restrict__ range, const int *__restrict__ rope,
             int *__restrict__ visits, Agg<R> *__restrict__ agg,
             typename RT<R>::R4 *__restrict__ rec_c, int2 *__restrict__ rec_t,
-            int *__restrict__ status, int2 *__restrict__ hsz, int *__restrict__ spine)
+            int *__restrict__ status)
 {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k < n)
         climb<R, false>(k, n, psort, child, parent, range, rope, visits, agg, rec_c, rec_t,
-                        status, hsz, spine);
+                        status);
 }
 
 // The climbs of P leaves per thread, one after the other: with n/P threads
@@ -574,7 +554,7 @@ k_aggregate_multi(int n, const typename RT<R>::R4 *__restrict__ psort,
                   const int2 *__restrict__ range, const int *__restrict__ rope,
                   int *__restrict__ visits, Agg<R> *__restrict__ agg,
                   typename RT<R>::R4 *__restrict__ rec_c, int2 *__restrict__ rec_t,
-                  int *__restrict__ status, int2 *__restrict__ hsz, int *__restrict__ spine)
+            int *__restrict__ status)
 {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
 #pragma unroll 1
@@ -582,141 +562,7 @@ k_aggregate_multi(int n, const typename RT<R>::R4 *__restrict__ psort,
         const int k = CONTIG ? t * P + q : ((t >> 5) * P + q) * 32 + (t & 31);
         if (k < n)
             climb<R, false>(k, n, psort, child, parent, range, rope, visits, agg, rec_c, rec_t,
-                            status, hsz, spine);
-    }
-}
-
-// ---- 4d. the tree in preorder, for the walk (FP32) --------------------------
-// The walk visits a region only if its parent is a region of 9 nodes or
-// more (the root too); a region of at most 8 nodes is summed node by node
-// when too close, never opened. Those visitable regions and nodes, laid out
-// in preorder -- the order of the walk -- put the first child of a region
-// right after it: a walk that opens a region reads the next record, and one
-// that approximates it jumps past its subtree. Preorder sorts them by first
-// sorted node, then by size, largest first: the position of one is the
-// number of them starting before its first node, plus its rank in the chain
-// of left children starting there, which climb() counted (hsz, spine).
-
-constexpr int SPINE_BLOCK = 2048; // entries of spine per scan block (256 x 8)
-
-// The position of the last visitable region or node starting at each sorted
-// node: an inclusive prefix sum of spine, per block of 2048 entries into
-// lpi, the block totals summed by the last block into bb (exclusive); spine
-// is cleared for the next iteration. spine / lpi hold a whole number of
-// blocks (zero past n).
-static __global__ void __launch_bounds__(256)
-k_spine_scan(int *__restrict__ spine, int *__restrict__ lpi, int *__restrict__ bsum,
-             int *__restrict__ bb, unsigned *__restrict__ ticket)
-{
-    __shared__ int ws[8];
-    __shared__ int last;
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    int4 *sp = reinterpret_cast<int4 *>(spine) + (size_t) blockIdx.x * (SPINE_BLOCK / 4) +
-               2 * threadIdx.x;
-    int4 *lp = reinterpret_cast<int4 *>(lpi) + (size_t) blockIdx.x * (SPINE_BLOCK / 4) +
-               2 * threadIdx.x;
-    const int4 a = sp[0], b = sp[1];
-    sp[0] = make_int4(0, 0, 0, 0);
-    sp[1] = make_int4(0, 0, 0, 0);
-    int v[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
-#pragma unroll
-    for (int u = 1; u < 8; u++) v[u] += v[u - 1];
-    int incl = v[7];
-    for (int o = 1; o < 32; o <<= 1) {
-        const int y = __shfl_up_sync(0xffffffffu, incl, o);
-        if (lane >= o) incl += y;
-    }
-    if (lane == 31) ws[w] = incl;
-    __syncthreads();
-    int before = 0;
-    for (int k = 0; k < w; k++) before += ws[k];
-    const int excl = before + incl - v[7];
-    lp[0] = make_int4(excl + v[0], excl + v[1], excl + v[2], excl + v[3]);
-    lp[1] = make_int4(excl + v[4], excl + v[5], excl + v[6], excl + v[7]);
-    if (threadIdx.x == 255) {
-        bsum[blockIdx.x] = before + incl;
-        __threadfence();
-        last = atomicAdd(ticket, 1u) == gridDim.x - 1;
-    }
-    __syncthreads();
-    if (!last) return;
-    __threadfence();
-    // the last block: exclusive prefix of the block totals, in order
-    const int nb = gridDim.x, per = (nb + 255) / 256;
-    const int k0 = threadIdx.x * per, k1 = min(nb, k0 + per);
-    int run = 0;
-    for (int k = k0; k < k1; k++) run += __ldcg(bsum + k);
-    int tincl = run;
-    for (int o = 1; o < 32; o <<= 1) {
-        const int y = __shfl_up_sync(0xffffffffu, tincl, o);
-        if (lane >= o) tincl += y;
-    }
-    __syncthreads();
-    if (lane == 31) ws[w] = tincl;
-    __syncthreads();
-    int acc = 0;
-    for (int k = 0; k < w; k++) acc += ws[k];
-    acc += tincl - run;
-    for (int k = k0; k < k1; k++) {
-        bb[k] = acc;
-        acc += __ldcg(bsum + k);
-    }
-    if (threadIdx.x == 0) *ticket = 0u;
-}
-
-// The records of the walk in preorder: prec (cx, cy, m, size^2; a single
-// node's position and mass, and 0 -- or, with prevent_overlap, infinity,
-// so that its pair is always summed node by node), plink = (position after
-// the subtree) << 2 | kind (0 a region that may be opened, 1 one of at most
-// 8 nodes, 2 a single node), paux = the region or the node. Region r (one
-// thread each) writes the records of its two children when it may be
-// opened; the root writes its own. P = hsz[0].y records.
-static __global__ void __launch_bounds__(256)
-k_pre_scatter(int n, int adjust, const int2 *__restrict__ child, const int2 *__restrict__ range,
-              const int2 *__restrict__ hsz, const int *__restrict__ lpi,
-              const int *__restrict__ bb, const float4 *__restrict__ rec_c,
-              const float4 *__restrict__ psort, float4 *__restrict__ prec,
-              int *__restrict__ plink, int *__restrict__ paux, int *__restrict__ status)
-{
-    const int r = blockIdx.x * blockDim.x + threadIdx.x;
-    const int nl = n - 1;
-    if (r >= nl) return;
-    const int P = hsz[0].y;
-    if (P < 1 || P > 2 * n - 1) { // at most the n - 1 regions and n nodes
-        if (r == 0) atomicOr(status + ST_ERROR, ERR_BOUNDS);
-        return;
-    }
-    const int2 rg = range[r];
-    const bool open = rg.y - rg.x >= 8;
-    if (r != 0 && !open) return;
-    int xs[3], nx = 0;
-    if (r == 0) xs[nx++] = 0; // the root itself
-    if (open) {
-        const int2 c = child[r];
-        xs[nx++] = c.x;
-        xs[nx++] = c.y;
-    }
-    for (int u = 0; u < nx; u++) {
-        const int x = xs[u];
-        const bool leaf = x >= nl && u > 0; // (the root is a region)
-        const int f = leaf ? x - nl : range[x].x;
-        const int2 hs = leaf ? make_int2(0, 1) : hsz[x];
-        const int pre = bb[f / SPINE_BLOCK] + lpi[f] - 1 - hs.x;
-        if (pre < 0 || pre >= P || pre + hs.y > P) {
-            atomicOr(status + ST_ERROR, ERR_BOUNDS);
-            continue;
-        }
-        if (leaf) {
-            const float4 p = psort[x - nl];
-            prec[pre] = make_float4(p.x, p.y, p.z, adjust ? __int_as_float(0x7f800000) : 0.0f);
-            plink[pre] = ((pre + 1) << 2) | 2;
-            paux[pre] = x - nl;
-        } else {
-            const int2 xr = range[x];
-            prec[pre] = rec_c[x];
-            plink[pre] = ((pre + hs.y) << 2) | (xr.y - xr.x >= 8 ? 0 : 1);
-            paux[pre] = x;
-        }
+                            status);
     }
 }
 
@@ -950,82 +796,6 @@ k_traverse_deferred(int n, R scaling, R theta2, double theta2d,
     if (k >= n) return;
     f[order[k]] = walk_deferred<R, ADJUST>(k, n, scaling, theta2, theta2d, psort, rec_c, rec_t,
                                            agg, rope, status);
-}
-
-// The walk over the preorder records (FP32), its node pairs deferred as in
-// walk_deferred: regions visited in the same order with the same decisions;
-// a single node whose pair can be approximated (no prevent_overlap, not
-// coincident) is taken like a far region -- its force is the pair's -- so
-// only the pairs of the small regions too close, and of coincident or
-// overlapping nodes, are queued.
-template <bool ADJUST>
-__global__ void __launch_bounds__(256, ADJUST ? 6 : 8)
-k_traverse_pre(int n, float scaling, float theta2, double theta2d,
-               const float4 *__restrict__ psort, const float4 *__restrict__ prec,
-               const int *__restrict__ plink, const int *__restrict__ paux,
-               const int2 *__restrict__ range, const Agg<float> *__restrict__ agg,
-               const int2 *__restrict__ hsz, const uint32_t *__restrict__ order,
-               float2 *__restrict__ f, int *__restrict__ status)
-{
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= n) return;
-    const float4 me = psort[k];
-    const float xi = me.x, yi = me.y, mi = me.z, si = me.w;
-    float ax = 0.0f, ay = 0.0f;
-    int P = hsz[0].y;
-    if (P < 1 || P > 2 * n - 1) {
-        atomicOr(status + ST_ERROR, ERR_BOUNDS);
-        P = 0;
-    }
-    int q[DEFER_QUEUE];
-    int nq = 0;
-    int cur = 0;
-    for (int step = 0; cur < P; step++) {
-        if (cur < 0 || step > P) {
-            atomicOr(status + ST_ERROR, ERR_BOUNDS);
-            break;
-        }
-        const float4 c = prec[cur];
-        const int l = plink[cur];
-        const float xd = xi - c.x, yd = yi - c.y;
-        const float d2 = xd * xd + yd * yd;
-        const float lhs = d2 * theta2;
-        bool far = lhs > c.w;
-        // (a single node's 0 or infinity is never in the band)
-        if (fabsf(lhs - c.w) < DECIDE_BAND * c.w)
-            far = far_dd(agg + paux[cur], xi, yi, theta2d);
-        if (far) {
-            const float g = fdiv(scaling * (mi * c.z), d2);
-            ax += xd * g;
-            ay += yd * g;
-            cur = l >> 2;
-            continue;
-        }
-        if ((l & 3) == 0) {
-            cur++;
-            continue;
-        }
-        const int a = paux[cur];
-        int bucket;
-        if ((l & 3) == 2) {
-            bucket = bucket_pack(a, a);
-        } else {
-            const int2 rg = range[a];
-            bucket = bucket_pack(rg.x, rg.y);
-        }
-        if (bucket_last(bucket) >= n || bucket_first(bucket) < 0) {
-            atomicOr(status + ST_ERROR, ERR_BOUNDS);
-            break;
-        }
-        if (nq == DEFER_QUEUE) {
-            sum_pairs<float, ADJUST>(k, q, nq, xi, yi, mi, si, scaling, psort, ax, ay);
-            nq = 0;
-        }
-        q[nq++] = bucket;
-        cur = l >> 2;
-    }
-    sum_pairs<float, ADJUST>(k, q, nq, xi, yi, mi, si, scaling, psort, ax, ay);
-    f[order[k]] = make_float2(ax, ay);
 }
 
 // The walk of P sorted nodes k0 .. k0+cnt-1 (cnt <= P, neighbours in

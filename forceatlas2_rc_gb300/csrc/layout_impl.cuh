@@ -124,13 +124,6 @@ template <class R> struct Layout : LayoutBase {
     Agg<R> *agg = nullptr;
     R4 *rec_c = nullptr; // traversal records (common.cuh)
     int2 *rec_t = nullptr;
-    // FP32: the preorder layout of the walk (k_spine_scan, k_pre_scatter)
-    int2 *hsz = nullptr;                   // per region: (h, s)
-    int *spine = nullptr, *lpi = nullptr;  // npad entries each
-    int *bsum = nullptr, *bb = nullptr;    // npad / SPINE_BLOCK each
-    float4 *prec = nullptr;                // 2n - 1 records at most
-    int *plink = nullptr, *paux = nullptr;
-    int npad = 0;
     double2 *swing_partial = nullptr;
     SpeedState *st = nullptr;
     int *status = nullptr;
@@ -196,17 +189,6 @@ template <class R> struct Layout : LayoutBase {
             agg = mem.get<Agg<R>>(nn - 1);
             rec_c = mem.get<R4>(nn - 1);
             rec_t = mem.get<int2>(nn - 1);
-            if (sizeof(R) == 4) {
-                npad = ceil_div(n, SPINE_BLOCK) * SPINE_BLOCK;
-                hsz = mem.get<int2>(nn - 1);
-                spine = mem.get<int>((size_t) npad);
-                lpi = mem.get<int>((size_t) npad);
-                bsum = mem.get<int>((size_t) npad / SPINE_BLOCK);
-                bb = mem.get<int>((size_t) npad / SPINE_BLOCK);
-                prec = mem.get<float4>(2 * nn - 1);
-                plink = mem.get<int>(2 * nn - 1);
-                paux = mem.get<int>(2 * nn - 1);
-            }
         } else {
             packed = mem.get<R4>(nn);
             if (exact_nrows > 1) exact_part = mem.get<R2>((size_t) exact_nrows * nn);
@@ -386,8 +368,6 @@ template <class R> struct Layout : LayoutBase {
         FA2_TRY(cudaMemsetAsync(fold, 0, (size_t) n * sizeof(R2), s), "cudaMemset", 1);
         FA2_TRY(cudaMemsetAsync(status, 0, ST_COUNT * sizeof(int), s), "cudaMemset", 1);
         if (repulsion == FA2CU_REPULSION_BH) sort_prepare(s, ss);
-        if (spine)
-            FA2_TRY(cudaMemsetAsync(spine, 0, (size_t) npad * sizeof(int), s), "cudaMemset", 1);
         if (set_positions(xy0)) return 1;
         SpeedState h{};
         h.speed = 1.0;
@@ -444,47 +424,34 @@ template <class R> struct Layout : LayoutBase {
     }
     void launch_tree()
     {
-        // the preorder layout of the walk: the climb counts, then two launches
-        const bool pre = walk == WALK_PREORDER && hsz;
-        int2 *ph = pre ? hsz : nullptr;
-        int *psp = pre ? spine : nullptr;
         k_gather_karras<R><<<ceil_div(n, 256), 256, 0, s>>>(n, adjust, order, pos, mass, size,
                                                             psort, key, child, range, parent,
                                                             rope, visits, status);
         switch (climb_mode) {
         case 2:
             k_aggregate_multi<R, 2, true><<<ceil_div(n, 512), 256, 0, s>>>(
-                n, psort, child, parent, range, rope, visits, agg, rec_c, rec_t, status, ph, psp);
+                n, psort, child, parent, range, rope, visits, agg, rec_c, rec_t, status);
             break;
         case 4:
             k_aggregate_multi<R, 4, true><<<ceil_div(n, 1024), 256, 0, s>>>(
-                n, psort, child, parent, range, rope, visits, agg, rec_c, rec_t, status, ph, psp);
+                n, psort, child, parent, range, rope, visits, agg, rec_c, rec_t, status);
             break;
         case 8:
             k_aggregate_multi<R, 8, true><<<ceil_div(n, 2048), 256, 0, s>>>(
-                n, psort, child, parent, range, rope, visits, agg, rec_c, rec_t, status, ph, psp);
+                n, psort, child, parent, range, rope, visits, agg, rec_c, rec_t, status);
             break;
         case -2:
             k_aggregate_multi<R, 2, false><<<ceil_div(n, 512), 256, 0, s>>>(
-                n, psort, child, parent, range, rope, visits, agg, rec_c, rec_t, status, ph, psp);
+                n, psort, child, parent, range, rope, visits, agg, rec_c, rec_t, status);
             break;
         case -4:
             k_aggregate_multi<R, 4, false><<<ceil_div(n, 1024), 256, 0, s>>>(
-                n, psort, child, parent, range, rope, visits, agg, rec_c, rec_t, status, ph, psp);
+                n, psort, child, parent, range, rope, visits, agg, rec_c, rec_t, status);
             break;
         default:
             k_aggregate<R><<<ceil_div(n, 256), 256, 0, s>>>(n, psort, child, parent, range,
                                                             rope, visits, agg, rec_c, rec_t,
-                                                            status, ph, psp);
-        }
-        if constexpr (sizeof(R) == 4) {
-            if (pre) {
-                k_spine_scan<<<npad / SPINE_BLOCK, 256, 0, s>>>(spine, lpi, bsum, bb,
-                                                               (unsigned *) (status + ST_TICKET_SPINE));
-                k_pre_scatter<<<ceil_div(n - 1, 256), 256, 0, s>>>(n, adjust, child, range, hsz, lpi,
-                                                                  bb, rec_c, psort, prec, plink,
-                                                                  paux, status);
-            }
+                                                            status);
         }
     }
     void launch_repulsion()
@@ -508,17 +475,6 @@ template <class R> struct Layout : LayoutBase {
                         <<<ceil_div(n, 256), 256, 0, s>>>(n, scaling, theta2, theta2d, psort,
                                                           rec_c, rec_t, agg, rope, order, f,
                                                           status);
-            } else if (walk == WALK_PREORDER) {
-                if constexpr (sizeof(R) == 4) {
-                    if (adjust)
-                        k_traverse_pre<true><<<ceil_div(n, 256), 256, 0, s>>>(
-                            n, scaling, theta2, theta2d, psort, prec, plink, paux, range, agg, hsz,
-                            order, f, status);
-                    else
-                        k_traverse_pre<false><<<ceil_div(n, 256), 256, 0, s>>>(
-                            n, scaling, theta2, theta2d, psort, prec, plink, paux, range, agg, hsz,
-                            order, f, status);
-                }
             } else if (walk == WALK_DEFERRED) {
                 if (adjust)
                     k_traverse_deferred<R, true, 6><<<ceil_div(n, 256), 256, 0, s>>>(
@@ -828,14 +784,9 @@ template <class R> struct Layout : LayoutBase {
             climb_mode = (int) value;
             return recapture();
         }
-        if (!strcmp(name, "walk") && value == WALK_PREORDER && sizeof(R) != 4) {
-            set_message("the preorder walk (6) is for single precision");
-            return 1;
-        }
         if (!strcmp(name, "walk") &&
             (value == WALK_WARP || value == WALK_THREAD || value == WALK_THREAD_WIDE ||
-             value == WALK_PAIR || value == WALK_QUAD || value == WALK_DEFERRED ||
-             value == WALK_PREORDER)) {
+             value == WALK_PAIR || value == WALK_QUAD || value == WALK_DEFERRED)) {
             walk = (int) value;
             return recapture();
         }

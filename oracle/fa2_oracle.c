@@ -798,11 +798,10 @@ void orc_pipe_tree(int n, const uint32_t *key, int *child, int *range,
 /* The float walk of that path: regions in float, but a region whose test
  * d^2 theta^2 > size^2 is within 1e-4 of the boundary is decided in double
  * from the double construction, so that the float path approximates the
- * regions the double path approximates. The forces of the far regions (and
- * of the single nodes taken like them) are added in walk order, then those
- * of the queued node pairs (the small regions too close, and the other
- * single nodes), in walk order: the order of the path's walk over the tree
- * in preorder (k_traverse_pre). */
+ * regions the double path approximates. The forces of the far regions are
+ * added in walk order, then those of the node pairs (the small regions too
+ * close and the single nodes), in walk order: the order of the path's walk,
+ * which queues the pairs (walk_deferred). */
 static void repulse_mixed(const pipe_ws_f *w, const pipe_ws_d *wd,
                           float scaling, float theta2, double theta2d,
                           int adjust, float *f)
@@ -824,19 +823,6 @@ static void repulse_mixed(const pipe_ws_f *w, const pipe_ws_d *wd,
             int first, last;
             if (r >= n - 1) {
                 first = last = r - (n - 1);
-                /* without prevent_overlap, a single node whose pair is not
-                 * coincident is taken like a far region (its force is the
-                 * pair's) in walk order; else its pair is queued */
-                if (!adjust) {
-                    const float xd = xi - ps[4 * first], yd = yi - ps[4 * first + 1];
-                    const float d2 = xd * xd + yd * yd;
-                    if (d2 * theta2 > 0.0f) {
-                        const float g = scaling * (mi * ps[4 * first + 2]) / d2;
-                        ax += xd * g;
-                        ay += yd * g;
-                        continue;
-                    }
-                }
             } else {
                 const float xd = xi - ni[4 * r], yd = yi - ni[4 * r + 1];
                 const float d2 = xd * xd + yd * yd;
