@@ -496,6 +496,10 @@ __device__ __forceinline__ void climb(int k, int n, const typename RT<R>::R4 *ps
 {
     const int nl = n - 1;
     int r = parent[nl + k];
+    // the sums of the child the thread comes from stay in registers: only
+    // the sibling's are loaded
+    int prev = nl + k;
+    Agg<R> mine = leaf_agg(psort[k]);
     // a Karras tree over 32-bit keys and n < 2^27 nodes is < 64 levels deep
     for (int depth = 0; r >= 0; depth++) {
         if (r >= nl || depth > 160) {
@@ -506,7 +510,8 @@ __device__ __forceinline__ void climb(int k, int n, const typename RT<R>::R4 *ps
         // the region's topology first (its links are known before its sums)
         const int2 c = child[r];
         const int2 rg = range[r];
-        if (c.x < 0 || c.y < 0 || c.x >= nl + n || c.y >= nl + n || rg.y < 0 || rg.y >= n) {
+        if (c.x < 0 || c.y < 0 || c.x >= nl + n || c.y >= nl + n || rg.y < 0 || rg.y >= n ||
+            (c.x != prev && c.y != prev)) {
             atomicOr(status + ST_ERROR, ERR_BOUNDS);
             return;
         }
@@ -514,12 +519,16 @@ __device__ __forceinline__ void climb(int k, int n, const typename RT<R>::R4 *ps
         // carries its packed range instead (negative)
         const int2 links =
             make_int2(rg.y - rg.x >= 8 ? c.x : bucket_pack(rg.x, rg.y), rope[rg.y]);
-        const Agg<R> a = c.x >= nl ? leaf_agg(psort[c.x - nl]) : load_agg_cg(agg + c.x);
-        const Agg<R> b = c.y >= nl ? leaf_agg(psort[c.y - nl]) : load_agg_cg(agg + c.y);
-        const Agg<R> q = agg_combine(a, b);
+        const bool from_a = c.x == prev;
+        const int other = from_a ? c.y : c.x;
+        const Agg<R> o = other >= nl ? leaf_agg(psort[other - nl]) : load_agg_cg(agg + other);
+        // a then b, whichever arrived last
+        const Agg<R> q = from_a ? agg_combine(mine, o) : agg_combine(o, mine);
         agg[r] = q;
         rec_c[r] = agg_record(q);
         rec_t[r] = links;
+        mine = q;
+        prev = r;
         r = parent[r];
     }
 }
@@ -1069,6 +1078,19 @@ constexpr int HEAVY_DEGREE = 128;
 // mass, size (node indices of inc are relative to them), added to the
 // repulsion already in f[i]. SKIP_HEAVY: a node of HEAVY_DEGREE incidences
 // or more gets its gravity only (k_attract_heavy added its attraction).
+// An incidence, read once per iteration: streamed (evict first), so that the
+// ~100 MB of incidence lists do not push the positions the attraction
+// gathers out of L2.
+__device__ __forceinline__ Inc<float> load_inc(const Inc<float> *p)
+{
+    const int2 v = __ldcs(reinterpret_cast<const int2 *>(p));
+    Inc<float> c;
+    c.j = v.x;
+    c.coef = __int_as_float(v.y);
+    return c;
+}
+__device__ __forceinline__ Inc<double> load_inc(const Inc<double> *p) { return *p; }
+
 template <class R, bool SKIP_HEAVY = false>
 __device__ __forceinline__ void attract_one(int i, R gravity, int strong, int linlog, int adjust,
                                             const typename RT<R>::R2 *pos,
@@ -1104,7 +1126,7 @@ __device__ __forceinline__ void attract_one(int i, R gravity, int strong, int li
         Inc<R> c[U];
         typename RT<R>::R2 q[U];
 #pragma unroll
-        for (int u = 0; u < U; u++) c[u] = inc[e0 + u < e1 ? e0 + u : e0];
+        for (int u = 0; u < U; u++) c[u] = load_inc(inc + (e0 + u < e1 ? e0 + u : e0));
 #pragma unroll
         for (int u = 0; u < U; u++) q[u] = pos[c[u].j];
 #pragma unroll
