@@ -132,6 +132,8 @@ k_batch(int ngraphs, BatchGraph *graphs, const int *queue, int *next, int iterat
         const R scaling = (R) G->scaling, gravity = (R) G->gravity;
         const double theta2d = G->theta2d;
         const R theta2 = (R) theta2d;
+        // the FP32 records' scale of size^2 (region_far)
+        const R wscale = (R) ((1.0 + (double) DECIDE_BAND) / theta2d);
         R2 *pos = A.pos + b0, *f = A.f + b0, *fold = A.fold + b0;
         const R *mass = A.mass + b0;
         const R *size = A.size ? A.size + b0 : nullptr;
@@ -325,7 +327,7 @@ k_batch(int ngraphs, BatchGraph *graphs, const int *queue, int *next, int iterat
                     const int k = tid * per + q;
                     if (k < n)
                         climb<R, true>(k, n, psort, child, parent, range, rope, visits, agg,
-                                       rec_c, rec_t, status);
+                                       rec_c, rec_t, wscale, status);
                 }
                 __syncthreads();
                 phase(BP_SUMS);

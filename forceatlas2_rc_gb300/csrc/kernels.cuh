@@ -450,7 +450,7 @@ __device__ __forceinline__ Agg<float> agg_combine(const Agg<float> &a, const Agg
 // (cx, cy, m, size^2) of a region: the reference's finalize
 // (pipeline.cl:312-323); in double for the FP64 path, from the float-float
 // sums for the FP32 path.
-__device__ __forceinline__ double4_32a agg_record(const Agg<double> &q)
+__device__ __forceinline__ double4_32a agg_record(const Agg<double> &q, double /*wscale*/)
 {
     const double w = __dsub_rn(q.maxx, q.minx), h = __dsub_rn(q.maxy, q.miny);
     double4_32a c;
@@ -461,12 +461,15 @@ __device__ __forceinline__ double4_32a agg_record(const Agg<double> &q)
     return c;
 }
 
-__device__ __forceinline__ float4 agg_record(const Agg<float> &q)
+// In float, the record holds w = size^2 * wscale with wscale = (1 + B) /
+// theta^2 (B = DECIDE_BAND): the walk's opening test is then d^2 > w, with
+// the band of decisions made again in double right below it (region_far).
+__device__ __forceinline__ float4 agg_record(const Agg<float> &q, float wscale)
 {
     const float m = q.m.hi + q.m.lo;
     const float w = q.maxx - q.minx, h = q.maxy - q.miny;
     return make_float4(__fdiv_rn(q.mx.hi + q.mx.lo, m), __fdiv_rn(q.my.hi + q.my.lo, m), m,
-                       2.0f * (w * w + h * h));
+                       2.0f * (w * w + h * h) * wscale);
 }
 
 // Arrival at region r: returns the number of children that arrived before
@@ -492,7 +495,7 @@ __device__ __forceinline__ void climb(int k, int n, const typename RT<R>::R4 *ps
                                       const int2 *range,
                                       const int *rope, int *visits,
                                       Agg<R> *agg, typename RT<R>::R4 *rec_c, int2 *rec_t,
-                                      int *status)
+                                      R wscale, int *status)
 {
     const int nl = n - 1;
     int r = parent[nl + k];
@@ -525,7 +528,7 @@ __device__ __forceinline__ void climb(int k, int n, const typename RT<R>::R4 *ps
         // a then b, whichever arrived last
         const Agg<R> q = from_a ? agg_combine(mine, o) : agg_combine(o, mine);
         agg[r] = q;
-        rec_c[r] = agg_record(q);
+        rec_c[r] = agg_record(q, wscale);
         rec_t[r] = links;
         mine = q;
         prev = r;
@@ -539,13 +542,13 @@ k_aggregate(int n, const typename RT<R>::R4 *__restrict__ psort,
             const int2 *__restrict__ child, const int *__restrict__ parent,
             const int2 *__restrict__ range, const int *__restrict__ rope,
             int *__restrict__ visits, Agg<R> *__restrict__ agg,
-            typename RT<R>::R4 *__restrict__ rec_c, int2 *__restrict__ rec_t,
+            typename RT<R>::R4 *__restrict__ rec_c, int2 *__restrict__ rec_t, R wscale,
             int *__restrict__ status)
 {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k < n)
         climb<R, false>(k, n, psort, child, parent, range, rope, visits, agg, rec_c, rec_t,
-                        status);
+                        wscale, status);
 }
 
 // The climbs of P leaves per thread, one after the other: with n/P threads
@@ -562,8 +565,8 @@ k_aggregate_multi(int n, const typename RT<R>::R4 *__restrict__ psort,
                   const int2 *__restrict__ child, const int *__restrict__ parent,
                   const int2 *__restrict__ range, const int *__restrict__ rope,
                   int *__restrict__ visits, Agg<R> *__restrict__ agg,
-                  typename RT<R>::R4 *__restrict__ rec_c, int2 *__restrict__ rec_t,
-            int *__restrict__ status)
+                  typename RT<R>::R4 *__restrict__ rec_c, int2 *__restrict__ rec_t, R wscale,
+                  int *__restrict__ status)
 {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
 #pragma unroll 1
@@ -571,7 +574,7 @@ k_aggregate_multi(int n, const typename RT<R>::R4 *__restrict__ psort,
         const int k = CONTIG ? t * P + q : ((t >> 5) * P + q) * 32 + (t & 31);
         if (k < n)
             climb<R, false>(k, n, psort, child, parent, range, rope, visits, agg, rec_c, rec_t,
-                            status);
+                            wscale, status);
     }
 }
 
@@ -613,6 +616,28 @@ __device__ __forceinline__ bool far_dd(const Agg<float> *a, float xi, float yi, 
 __device__ __forceinline__ bool far_dd(const Agg<double> *a, float xi, float yi, double theta2d)
 {
     return false; // the FP64 walk decides in double directly
+}
+
+// The opening test d^2 theta^2 > size^2 of a region (pipeline.cl:350). The
+// FP64 records hold size^2 and the test is made as stated. The FP32 records
+// hold w = size^2 (1 + B) / theta^2, the top of the band of relative width B
+// around the boundary: a region beyond it is far; one inside the band (d^2
+// above w (1 - B) / (1 + B)) is decided again in double; the rest are near.
+// (theta = 0: w is infinite, or not a number for a region of size 0, and
+// every region is near.)
+constexpr float DECIDE_LO = (1.0f - DECIDE_BAND) / (1.0f + DECIDE_BAND);
+__device__ __forceinline__ bool region_far(float d2, float w, float /*theta2*/,
+                                           const Agg<float> *a, float xi, float yi,
+                                           double theta2d)
+{
+    if (d2 > w) return true;
+    if (d2 > w * DECIDE_LO) return far_dd(a, xi, yi, theta2d);
+    return false;
+}
+__device__ __forceinline__ bool region_far(double d2, double w, double theta2,
+                                           const Agg<double> *, float, float, double)
+{
+    return d2 * theta2 > w;
 }
 
 // The force of the tree's walk on sorted node k of an n-node tree.
@@ -661,10 +686,7 @@ walk(int k, int n, R scaling, R theta2, double theta2d,
         const int2 t = rec_t[cur];
         const R xd = xi - c.x, yd = yi - c.y;
         const R d2 = xd * xd + yd * yd;
-        const R lhs = d2 * theta2;
-        bool far = lhs > c.w;
-        if (sizeof(R) == 4 && fabs_r(lhs - c.w) <= R(DECIDE_BAND) * c.w)
-            far = far_dd(agg + cur, (float) xi, (float) yi, theta2d);
+        const bool far = region_far(d2, c.w, theta2, agg + cur, (float) xi, (float) yi, theta2d);
         if (far) {
             const R g = fdiv(scaling * (mi * c.z), d2);
             ax += xd * g;
@@ -760,10 +782,8 @@ walk_deferred(int k, int n, R scaling, R theta2, double theta2d,
             const int2 t = rec_t[cur];
             const R xd = xi - c.x, yd = yi - c.y;
             const R d2 = xd * xd + yd * yd;
-            const R lhs = d2 * theta2;
-            bool far = lhs > c.w;
-            if (sizeof(R) == 4 && fabs_r(lhs - c.w) <= R(DECIDE_BAND) * c.w)
-                far = far_dd(agg + cur, (float) xi, (float) yi, theta2d);
+            const bool far =
+                region_far(d2, c.w, theta2, agg + cur, (float) xi, (float) yi, theta2d);
             if (far) {
                 const R g = fdiv(scaling * (mi * c.z), d2);
                 ax += xd * g;
@@ -882,10 +902,8 @@ walk_multi(int k0, int cnt, int n, R scaling, R theta2, double theta2d,
             if (!((act >> u) & 1u)) continue;
             const R xd = xi[u] - c.x, yd = yi[u] - c.y;
             const R d2 = xd * xd + yd * yd;
-            const R lhs = d2 * theta2;
-            bool far = lhs > c.w;
-            if (sizeof(R) == 4 && fabs_r(lhs - c.w) <= R(DECIDE_BAND) * c.w)
-                far = far_dd(agg + cur, (float) xi[u], (float) yi[u], theta2d);
+            const bool far =
+                region_far(d2, c.w, theta2, agg + cur, (float) xi[u], (float) yi[u], theta2d);
             if (far) {
                 const R g = fdiv(scaling * (mi[u] * c.z), d2);
                 ax[u] += xd * g;
@@ -983,10 +1001,8 @@ k_traverse_warp(int n, R scaling, R theta2, double theta2d,
         if (rg.x >= resume) {
             const R xd = xi - c.x, yd = yi - c.y;
             const R d2 = xd * xd + yd * yd;
-            const R lhs = d2 * theta2;
-            bool far = lhs > c.w;
-            if (sizeof(R) == 4 && fabs_r(lhs - c.w) <= R(DECIDE_BAND) * c.w)
-                far = far_dd(agg + cur, (float) xi, (float) yi, theta2d);
+            const bool far =
+                region_far(d2, c.w, theta2, agg + cur, (float) xi, (float) yi, theta2d);
             if (far) {
                 const R g = fdiv(scaling * (mi * c.z), d2);
                 ax += xd * g;
@@ -1042,10 +1058,8 @@ k_traverse_count(int n, R theta2, double theta2d, const typename RT<R>::R4 *__re
             const int2 t = rec_t[cur];
             const R xd = me.x - c.x, yd = me.y - c.y;
             const R d2 = xd * xd + yd * yd;
-            const R lhs = d2 * theta2;
-            bool far = lhs > c.w;
-            if (sizeof(R) == 4 && fabs_r(lhs - c.w) <= R(DECIDE_BAND) * c.w)
-                far = far_dd(agg + cur, (float) me.x, (float) me.y, theta2d);
+            const bool far =
+                region_far(d2, c.w, theta2, agg + cur, (float) me.x, (float) me.y, theta2d);
             if (far) {
                 cur = t.y;
             } else if (t.x >= 0) {

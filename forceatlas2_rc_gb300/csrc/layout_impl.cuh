@@ -98,6 +98,7 @@ template <class R> struct Layout : LayoutBase {
         return x < 1.0 ? 1 : 2;
     }
     R scaling = 0, gravity = 0, theta2 = 0;
+    R wscale = 0; // FP32 records: size^2 (1 + DECIDE_BAND) / theta^2 (region_far)
     double theta2d = 0.0;
     cudaStream_t s = nullptr;
     DevMem mem;
@@ -279,6 +280,7 @@ template <class R> struct Layout : LayoutBase {
         gravity = (R) p->gravity;
         theta2d = p->theta * p->theta;
         theta2 = (R) theta2d;
+        wscale = (R) ((1.0 + (double) DECIDE_BAND) / theta2d);
         if (opts && opts->has_priority)
             FA2_TRY(cudaStreamCreateWithPriority(&s, cudaStreamNonBlocking, opts->priority),
                     "could not create a CUDA stream", 1);
@@ -430,28 +432,28 @@ template <class R> struct Layout : LayoutBase {
         switch (climb_mode) {
         case 2:
             k_aggregate_multi<R, 2, true><<<ceil_div(n, 512), 256, 0, s>>>(
-                n, psort, child, parent, range, rope, visits, agg, rec_c, rec_t, status);
+                n, psort, child, parent, range, rope, visits, agg, rec_c, rec_t, wscale, status);
             break;
         case 4:
             k_aggregate_multi<R, 4, true><<<ceil_div(n, 1024), 256, 0, s>>>(
-                n, psort, child, parent, range, rope, visits, agg, rec_c, rec_t, status);
+                n, psort, child, parent, range, rope, visits, agg, rec_c, rec_t, wscale, status);
             break;
         case 8:
             k_aggregate_multi<R, 8, true><<<ceil_div(n, 2048), 256, 0, s>>>(
-                n, psort, child, parent, range, rope, visits, agg, rec_c, rec_t, status);
+                n, psort, child, parent, range, rope, visits, agg, rec_c, rec_t, wscale, status);
             break;
         case -2:
             k_aggregate_multi<R, 2, false><<<ceil_div(n, 512), 256, 0, s>>>(
-                n, psort, child, parent, range, rope, visits, agg, rec_c, rec_t, status);
+                n, psort, child, parent, range, rope, visits, agg, rec_c, rec_t, wscale, status);
             break;
         case -4:
             k_aggregate_multi<R, 4, false><<<ceil_div(n, 1024), 256, 0, s>>>(
-                n, psort, child, parent, range, rope, visits, agg, rec_c, rec_t, status);
+                n, psort, child, parent, range, rope, visits, agg, rec_c, rec_t, wscale, status);
             break;
         default:
             k_aggregate<R><<<ceil_div(n, 256), 256, 0, s>>>(n, psort, child, parent, range,
                                                             rope, visits, agg, rec_c, rec_t,
-                                                            status);
+                                                            wscale, status);
         }
     }
     void launch_repulsion()
@@ -734,6 +736,7 @@ template <class R> struct Layout : LayoutBase {
         launch_sort();
         launch_tree();
         std::vector<R4> hc((size_t) n - 1);
+        std::vector<Agg<R>> ha(sizeof(R) == 4 ? (size_t) n - 1 : 0);
         const size_t nn = (size_t) n;
         cudaMemcpyAsync(hkey, key, nn * 4, cudaMemcpyDeviceToHost, s);
         cudaMemcpyAsync(horder, order, nn * 4, cudaMemcpyDeviceToHost, s);
@@ -741,12 +744,20 @@ template <class R> struct Layout : LayoutBase {
         cudaMemcpyAsync(hrange, range, (nn - 1) * sizeof(int2), cudaMemcpyDeviceToHost, s);
         cudaMemcpyAsync(hparent, parent, (2 * nn - 1) * sizeof(int), cudaMemcpyDeviceToHost, s);
         cudaMemcpyAsync(hc.data(), rec_c, (nn - 1) * sizeof(R4), cudaMemcpyDeviceToHost, s);
+        if (sizeof(R) == 4)
+            cudaMemcpyAsync(ha.data(), agg, (nn - 1) * sizeof(Agg<R>), cudaMemcpyDeviceToHost, s);
         FA2_TRY(cudaStreamSynchronize(s), "could not fetch the tree", 1);
         for (size_t r = 0; r + 1 < nn; r++) {
             hni[4 * r] = (double) hc[r].x;
             hni[4 * r + 1] = (double) hc[r].y;
             hni[4 * r + 2] = (double) hc[r].z;
-            hni[4 * r + 3] = (double) hc[r].w;
+            if (sizeof(R) == 4) { // the FP32 record holds a scaled size^2 (region_far)
+                const float w = (float) (ha[r].maxx - ha[r].minx);
+                const float h = (float) (ha[r].maxy - ha[r].miny);
+                hni[4 * r + 3] = (double) (2.0f * (w * w + h * h));
+            } else {
+                hni[4 * r + 3] = (double) hc[r].w;
+            }
         }
         return 0;
     }
