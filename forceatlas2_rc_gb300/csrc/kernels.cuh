@@ -767,9 +767,10 @@ walk_deferred(int k, int n, R scaling, R theta2, double theta2d,
     int cur = 0;
     // one step per region (n - 1) and per single node reached as a leaf (n)
     const int cap = 2 * n + 64;
-    for (int step = 0; cur != -1; step++) {
+    for (int step = 0;; step++) {
+        // the end of the walk (-1), or a link out of range
         if ((unsigned) cur >= nend || step > cap) {
-            atomicOr(status + ST_ERROR, ERR_BOUNDS);
+            if (cur != -1) atomicOr(status + ST_ERROR, ERR_BOUNDS);
             break;
         }
         int bucket;
