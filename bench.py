@@ -67,8 +67,8 @@ TRAVERSE_L2_BYTES_PER_PAIR = 16
 # DRAM bytes (read + write) of one traversal launch on this workload
 # (dram__bytes_read.sum + dram__bytes_write.sum, one ncu capture of each
 # walk), and the share of cycles the schedulers issued (the kernel's bound)
-TRAVERSE_DRAM_BYTES = {"deferred": 51.76e6 + 3.21e6, "thread": 45.94e6 + 0.86e6}
-TRAVERSE_ISSUE_ACTIVE = {"deferred": 0.816, "thread": 0.805}
+TRAVERSE_DRAM_BYTES = {"deferred": 51.79e6 + 2.92e6, "thread": 45.94e6 + 0.86e6}
+TRAVERSE_ISSUE_ACTIVE = {"deferred": 0.788, "thread": 0.805}
 
 
 def make_workload(small: bool = False):
