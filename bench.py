@@ -320,18 +320,34 @@ def full_run_e2e(g, pos, iters, local, calls=2, linlog=False, outbound=False):
 
 # ---- the CPU legs: the reference's engine on the host cores ----------------
 
-def cpu_sample(n, a, b, w, pos, iters, threads, linlog, outbound):
-    """The reference's CPU engine (C_forceatlas2 with the Gephi quadtree,
-    the oracle's restatement) on this host: node-iterations/s over `iters`
-    iterations after one warm-up iteration."""
+def cpu_engine():
+    """Which build of the reference's CPU engine this host can run:
+    "reference", the package's own src/forceatlas2.c compiled from its
+    sources (oracle/_ref, where it was built for this machine), else "port",
+    the oracle's restatement (bit-identical to it on every golden case)."""
     import oracle
+    try:
+        if oracle.ref_lib() is not None:
+            return "reference"
+    except OSError:  # built for another machine
+        pass
+    return "port"
+
+
+def cpu_sample(n, a, b, w, pos, iters, threads, linlog, outbound):
+    """The reference's CPU engine (C_forceatlas2 with the Gephi quadtree) on
+    this host: node-iterations/s over `iters` iterations after one warm-up
+    iteration, and which build ran (cpu_engine)."""
+    import oracle
+    kind = cpu_engine()
+    which = "ref" if kind == "reference" else "oracle"
     o = oracle.Opts(scaling=2.0, gravity=1.0, linlog=linlog, outbound=outbound,
                     barnes_hut=True, theta=1.2, threads=threads)
-    p1 = oracle.layout(n, a, b, w, pos, None, None, 1, o)
+    p1 = oracle.layout(n, a, b, w, pos, None, None, 1, o, which=which)
     t0 = time.perf_counter()
-    oracle.layout(n, a, b, w, p1, None, None, iters, o)
+    oracle.layout(n, a, b, w, p1, None, None, iters, o, which=which)
     dt = time.perf_counter() - t0
-    return n * iters / dt, dt
+    return n * iters / dt, dt, kind
 
 
 def gpu_mode_leg(local):
@@ -420,11 +436,11 @@ def cpu_legs(args, heads):
     from forceatlas2_rc_gb300 import graphs
     pos = graphs.uniform_positions(n, -r, r, seed=2)
     iters = 10 if args.small else 40
-    cv, cdt = cpu_sample(n, a, b, np.ones(len(a)), pos, iters, threads, True, True)
+    cv, cdt, kind = cpu_sample(n, a, b, np.ones(len(a)), pos, iters, threads, True, True)
     t0 = time.perf_counter()
     oracle.prepare_large(n, a, b, np.ones(len(a)), outbound=True)
     prep_s = time.perf_counter() - t0
-    out["sbm"] = {"value": cv, "unit": UNIT, "cores": threads, "kind": "port",
+    out["sbm"] = {"value": cv, "unit": UNIT, "cores": threads, "kind": kind,
                   "sample": f"{iters} iterations of the full {n}-node workload (after 1 "
                             f"warm-up), C_forceatlas2 quadtree engine, {cdt:.1f} s",
                   "graph_prep_s": prep_s,
@@ -432,8 +448,8 @@ def cpu_legs(args, heads):
                                 "lists), oracle restatement, 1 core"}
     if "ba" in heads:
         n, a, b, w, pos = heads["ba"]
-        cv, cdt = cpu_sample(n, a, b, w, pos, 50, threads, False, False)
-        out["ba"] = {"value": cv, "unit": UNIT, "cores": threads, "kind": "port",
+        cv, cdt, kind = cpu_sample(n, a, b, w, pos, 50, threads, False, False)
+        out["ba"] = {"value": cv, "unit": UNIT, "cores": threads, "kind": kind,
                      "sample": f"50 iterations of the {n}-node workload (after 1 warm-up), "
                                f"C_forceatlas2 quadtree engine, {cdt:.1f} s"}
     if heads.get("gpu_mode"):
@@ -451,6 +467,8 @@ def run_reference(args):
     import oracle
     oracle.build()
     threads = os.cpu_count() or 1
+    kind = cpu_engine()
+    which = "ref" if kind == "reference" else "oracle"
     n, a, b, _ = make_workload(args.small)
     w = np.ones(len(a))
     o = oracle.Opts(scaling=2.0, gravity=1.0, linlog=True, outbound=True,
@@ -458,9 +476,9 @@ def run_reference(args):
     r = 10.0 * np.sqrt(n)
     from forceatlas2_rc_gb300 import graphs
     pos = graphs.uniform_positions(n, -r, r, seed=2)
-    pos = oracle.layout(n, a, b, w, pos, None, None, args.warmup, o)
+    pos = oracle.layout(n, a, b, w, pos, None, None, args.warmup, o, which=which)
     t0 = time.perf_counter()
-    oracle.layout(n, a, b, w, pos, None, None, args.steps, o)
+    oracle.layout(n, a, b, w, pos, None, None, args.steps, o, which=which)
     dt = time.perf_counter() - t0
     value = n * args.steps / dt
     line = {
@@ -471,9 +489,11 @@ def run_reference(args):
         "data": "synthetic",
         "config": {"workload": WORKLOAD, "n": n, "edges": int(len(a)),
                    "engine": "src/forceatlas2.c C_forceatlas2 loop (quadtree "
-                             "Barnes-Hut, OpenMP), oracle restatement"},
+                             "Barnes-Hut, OpenMP), " +
+                             ("compiled from the reference's sources" if kind == "reference"
+                              else "oracle restatement")},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads,
-                         "kind": "port",
+                         "kind": kind,
                          "sample": f"{args.steps} iterations of the full "
                                    f"workload after {args.warmup} warm-up"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
@@ -603,8 +623,8 @@ def run_ba(args):
         import oracle
         oracle.build()
         n, a, b, w, pos = work
-        cv, cdt = cpu_sample(n, a, b, w, pos, 50, os.cpu_count() or 1, False, False)
-        cpu = {"value": cv, "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",
+        cv, cdt, kind = cpu_sample(n, a, b, w, pos, 50, os.cpu_count() or 1, False, False)
+        cpu = {"value": cv, "unit": UNIT, "cores": os.cpu_count() or 1, "kind": kind,
                "sample": f"50 iterations (after 1 warm-up), C_forceatlas2 quadtree "
                          f"engine, {cdt:.1f} s"}
     line = {"metric": METRIC, "value": r["value"], "unit": UNIT, "n_gpus": 1,

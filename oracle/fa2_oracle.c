@@ -92,8 +92,19 @@ static inline int one_quadrant(const int *c, int count)
 void orc_tree_build(fa2_tree *t, int n, const double *x, const double *y,
                     const double *mass, const double *size)
 {
-    /* src/forceatlas2.c:64-239, breadth first, one level at a time. */
+    orc_tree_build_mt(t, n, x, y, mass, size, 1);
+}
+
+void orc_tree_build_mt(fa2_tree *t, int n, const double *x, const double *y,
+                       const double *mass, const double *size, int threads)
+{
+    /* src/forceatlas2.c:64-239, breadth first, one level at a time; the
+     * regions of a level in parallel as there (:104-108, :166-168,
+     * :220-221): the tree does not depend on the number of threads. */
     fa2_region *R = t->reg;
+#ifndef _OPENMP
+    (void) threads;
+#endif
 
     {   /* the root: every node, in index order (:74-97) */
         fa2_node *nd = t->buf[0];
@@ -122,7 +133,14 @@ void orc_tree_build(fa2_tree *t, int n, const double *x, const double *y,
 
     int lo = 0, hi = 1;
     while (lo < hi) {
+#ifdef _OPENMP
+        int chunk = (hi - lo) / (8 * (threads > 0 ? threads : 1));
+        if (chunk < 1) chunk = 1;
+#endif
         /* (1) size of each region and its quadrant counts (:106-126) */
+#ifdef _OPENMP
+#pragma omp parallel for num_threads(threads) schedule(dynamic, chunk) if (threads > 1 && hi - lo > 1)
+#endif
         for (int r = lo; r < hi; r++) {
             int *c = t->cnt + 4 * (size_t) (r - lo);
             c[0] = c[1] = c[2] = c[3] = 0;
@@ -177,6 +195,9 @@ void orc_tree_build(fa2_tree *t, int n, const double *x, const double *y,
         }
 
         /* (3) move the nodes to their quadrant; masses and centres (:166-216) */
+#ifdef _OPENMP
+#pragma omp parallel for num_threads(threads) schedule(dynamic, chunk) if (threads > 1 && hi - lo > 1)
+#endif
         for (int r = lo; r < hi; r++) {
             const int *c = t->cnt + 4 * (size_t) (r - lo);
             if (R[r].nchild == 0) continue;
@@ -223,6 +244,9 @@ void orc_tree_build(fa2_tree *t, int n, const double *x, const double *y,
     }
 
     /* nodes in tree order, from the buffer that holds each leaf (:222-238) */
+#ifdef _OPENMP
+#pragma omp parallel for num_threads(threads) schedule(static) if (threads > 1)
+#endif
     for (int r = 0; r < t->nreg; r++) {
         if (R[r].nchild > 0) continue;
         const fa2_node *nd = t->buf[R[r].buf];
@@ -443,7 +467,7 @@ int orc_forces(int n, int m, const int *from, const int *to, const double *w,
             free(mass);
             return 1;
         }
-        orc_tree_build(&t, n, x, y, mass, o->adjust ? size : NULL);
+        orc_tree_build_mt(&t, n, x, y, mass, o->adjust ? size : NULL, thr);
         orc_repulse_bh(n, &t, x, y, mass, size, o->adjust, o->scaling,
                        o->theta, thr, dx, dy);
         tree_free(&t);
@@ -570,7 +594,7 @@ static int layout_impl(int n, int m, const int *from, const int *to,
         memset(dy, 0, nn * sizeof(double));
 
         if (o->barnes_hut) {
-            orc_tree_build(&t, n, x, y, mass, o->adjust ? size : NULL);
+            orc_tree_build_mt(&t, n, x, y, mass, o->adjust ? size : NULL, threads);
             orc_repulse_bh(n, &t, x, y, mass, size, o->adjust, o->scaling,
                            o->theta, threads, dx, dy);
         } else {

@@ -50,6 +50,9 @@ void orc_repulse_exact(int n, const double *x, const double *y,
  * t->px/py/pm (n) and t->ps (n, or NULL when size is NULL). */
 void orc_tree_build(fa2_tree *t, int n, const double *x, const double *y,
                     const double *mass, const double *size);
+/* The same with the regions of a level on `threads` OpenMP threads. */
+void orc_tree_build_mt(fa2_tree *t, int n, const double *x, const double *y,
+                       const double *mass, const double *size, int threads);
 
 /* Barnes-Hut repulsion over that tree, ADDED to dx, dy
  * (src/forceatlas2.c:320-368). */
