@@ -194,7 +194,7 @@ class QuadTree:
     """A Gephi quadtree built by the oracle, in fa2_tree layout (the input of
     fa2_gpu_repulse_bh). Keeps its arrays alive."""
 
-    def __init__(self, n, pos, mass_, size=None):
+    def __init__(self, n, pos, mass_, size=None, threads=1):
         self.n = n
         xy = _pos_cols(pos)
         self._x, self._y = xy[:n].copy(), xy[n:].copy()
@@ -218,8 +218,8 @@ class QuadTree:
         t.px, t.py, t.pm = dptr(self.px), dptr(self.py), dptr(self.pm)
         t.ps = dptr(self.ps)
         self.t = t
-        lib().orc_tree_build(C.byref(t), n, dptr(self._x), dptr(self._y),
-                             dptr(self._m), dptr(self._s))
+        lib().orc_tree_build_mt(C.byref(t), n, dptr(self._x), dptr(self._y),
+                                dptr(self._m), dptr(self._s), int(threads))
 
     @property
     def nreg(self):
