@@ -732,10 +732,31 @@ k_traverse(int n, R scaling, R theta2, double theta2d,
 // another order: the far regions in walk order, then the pairs in walk order.
 constexpr int DEFER_QUEUE = 16;
 
+// A node of mass 1 + HEAVY_DEGREE or more (a hub) near equilibrium feels a
+// repulsion that nearly cancels an attraction ~100 times larger than the
+// net force: summed in plain float, the running sum's roundings reach
+// ~1e-4 of the largest net force. The walk adds its terms with Kahan
+// compensation for such nodes (in graphs that have any; COMP).
+constexpr float HUB_MASS = 1.0f + 128; // 1 + HEAVY_DEGREE (below)
+
+// s += v, compensated when `comp` (c carries the lost low part, negated).
+__device__ __forceinline__ void acc_add(float &s, float &c, float v, bool comp)
+{
+    if (comp) {
+        const float y = __fsub_rn(v, c);
+        const float t = __fadd_rn(s, y);
+        c = __fsub_rn(__fsub_rn(t, s), y);
+        s = t;
+    } else {
+        s += v;
+    }
+}
+__device__ __forceinline__ void acc_add(double &s, double &, double v, bool) { s += v; }
+
 template <class R, bool ADJUST>
 __device__ __forceinline__ void sum_pairs(int k, const int *q, int nq, R xi, R yi, R mi, R si,
                                           R scaling, const typename RT<R>::R4 *psort, R &ax,
-                                          R &ay)
+                                          R &ay, R &cx, R &cy, bool comp)
 {
     for (int b = 0; b < nq; b++) {
         const int last = bucket_last(q[b]);
@@ -744,13 +765,13 @@ __device__ __forceinline__ void sum_pairs(int k, const int *q, int nq, R xi, R y
             const typename RT<R>::R4 p = psort[j];
             const R xd = xi - p.x, yd = yi - p.y;
             const R g = rep_factor<R, ADJUST>(xd * xd + yd * yd, mi * p.z, si + p.w, scaling);
-            ax += xd * g;
-            ay += yd * g;
+            acc_add(ax, cx, xd * g, comp);
+            acc_add(ay, cy, yd * g, comp);
         }
     }
 }
 
-template <class R, bool ADJUST>
+template <class R, bool ADJUST, bool COMP = false>
 __device__ __forceinline__ typename RT<R>::R2
 walk_deferred(int k, int n, R scaling, R theta2, double theta2d,
               const typename RT<R>::R4 *psort, const typename RT<R>::R4 *rec_c,
@@ -759,7 +780,8 @@ walk_deferred(int k, int n, R scaling, R theta2, double theta2d,
     typedef typename RT<R>::R4 R4;
     const R4 me = psort[k];
     const R xi = me.x, yi = me.y, mi = me.z, si = me.w;
-    R ax = R(0), ay = R(0);
+    R ax = R(0), ay = R(0), cx = R(0), cy = R(0);
+    const bool comp = COMP && sizeof(R) == 4 && mi >= R(HUB_MASS);
     const int nl = n - 1;
     const unsigned nend = (unsigned) (nl + n);
     int q[DEFER_QUEUE];
@@ -787,8 +809,8 @@ walk_deferred(int k, int n, R scaling, R theta2, double theta2d,
                 region_far(d2, c.w, theta2, agg + cur, (float) xi, (float) yi, theta2d);
             if (far) {
                 const R g = fdiv(scaling * (mi * c.z), d2);
-                ax += xd * g;
-                ay += yd * g;
+                acc_add(ax, cx, xd * g, comp);
+                acc_add(ay, cy, yd * g, comp);
                 cur = t.y;
                 continue;
             }
@@ -804,16 +826,20 @@ walk_deferred(int k, int n, R scaling, R theta2, double theta2d,
             cur = t.y;
         }
         if (nq == DEFER_QUEUE) {
-            sum_pairs<R, ADJUST>(k, q, nq, xi, yi, mi, si, scaling, psort, ax, ay);
+            sum_pairs<R, ADJUST>(k, q, nq, xi, yi, mi, si, scaling, psort, ax, ay, cx, cy, comp);
             nq = 0;
         }
         q[nq++] = bucket;
     }
-    sum_pairs<R, ADJUST>(k, q, nq, xi, yi, mi, si, scaling, psort, ax, ay);
+    sum_pairs<R, ADJUST>(k, q, nq, xi, yi, mi, si, scaling, psort, ax, ay, cx, cy, comp);
+    if (comp) {
+        ax -= cx;
+        ay -= cy;
+    }
     return mk2<R>(ax, ay);
 }
 
-template <class R, bool ADJUST, int MINB>
+template <class R, bool ADJUST, int MINB, bool COMP = false>
 __global__ void __launch_bounds__(256, MINB)
 k_traverse_deferred(int n, R scaling, R theta2, double theta2d,
                     const typename RT<R>::R4 *__restrict__ psort,
@@ -824,8 +850,8 @@ k_traverse_deferred(int n, R scaling, R theta2, double theta2d,
 {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
-    f[order[k]] = walk_deferred<R, ADJUST>(k, n, scaling, theta2, theta2d, psort, rec_c, rec_t,
-                                           agg, rope, status);
+    f[order[k]] = walk_deferred<R, ADJUST, COMP>(k, n, scaling, theta2, theta2d, psort, rec_c,
+                                                 rec_t, agg, rope, status);
 }
 
 // The walk of P sorted nodes k0 .. k0+cnt-1 (cnt <= P, neighbours in
@@ -1088,6 +1114,7 @@ k_traverse_count(int n, R theta2, double theta2d, const typename RT<R>::R4 *__re
 // would hold up its whole launch. The FP64 path keeps one thread per node:
 // its sums follow the reference's edge order.
 constexpr int HEAVY_DEGREE = 128;
+static_assert(HUB_MASS == 1.0f + HEAVY_DEGREE, "hubs of the walk and of the attraction");
 
 // Gravity and attraction on node i of a graph whose arrays start at pos,
 // mass, size (node indices of inc are relative to them), added to the

@@ -478,14 +478,27 @@ template <class R> struct Layout : LayoutBase {
                                                           rec_c, rec_t, agg, rope, order, f,
                                                           status);
             } else if (walk == WALK_DEFERRED) {
-                if (adjust)
-                    k_traverse_deferred<R, true, 6><<<ceil_div(n, 256), 256, 0, s>>>(
-                        n, scaling, theta2, theta2d, psort, rec_c, rec_t, agg, rope, order, f, status);
-                else
-                    k_traverse_deferred<R, false, sizeof(R) == 4 ? 8 : 6>
-                        <<<ceil_div(n, 256), 256, 0, s>>>(n, scaling, theta2, theta2d, psort,
-                                                          rec_c, rec_t, agg, rope, order, f,
-                                                          status);
+                // graphs with hubs: their walks add up with compensation
+                const int g = ceil_div(n, 256);
+                if (adjust) {
+                    if (nheavy > 0)
+                        k_traverse_deferred<R, true, 6, true><<<g, 256, 0, s>>>(
+                            n, scaling, theta2, theta2d, psort, rec_c, rec_t, agg, rope, order, f,
+                            status);
+                    else
+                        k_traverse_deferred<R, true, 6><<<g, 256, 0, s>>>(
+                            n, scaling, theta2, theta2d, psort, rec_c, rec_t, agg, rope, order, f,
+                            status);
+                } else {
+                    if (nheavy > 0)
+                        k_traverse_deferred<R, false, sizeof(R) == 4 ? 8 : 6, true>
+                            <<<g, 256, 0, s>>>(n, scaling, theta2, theta2d, psort, rec_c, rec_t,
+                                               agg, rope, order, f, status);
+                    else
+                        k_traverse_deferred<R, false, sizeof(R) == 4 ? 8 : 6>
+                            <<<g, 256, 0, s>>>(n, scaling, theta2, theta2d, psort, rec_c, rec_t,
+                                               agg, rope, order, f, status);
+                }
             } else if (walk == WALK_PAIR) {
                 const int grid = ceil_div(ceil_div(n, 2), 256);
                 if (adjust)

@@ -460,3 +460,23 @@ def test_heavy_nodes_single(gpu, orc, opts):
     assert launches == launches_d + 1
     assert rel_err(f, orc.pipe_forces(p, pos, "m")) <= 1e-5
     assert rel_err(f, fd) <= (2e-3 if opts.get("adjust") else 1e-4)
+
+
+def test_fp32_forces_near_equilibrium_with_hubs(gpu):
+    """Near equilibrium a hub's repulsion and attraction nearly cancel (each
+    ~100 times the net force); the FP32 walk adds the terms of hubs (mass
+    129 or more) with Kahan compensation, which keeps the FP32 forces within
+    1e-4 of the FP64 forces at the FP32 layout's own positions after 400
+    iterations (Barabasi-Albert, 20,000 nodes, lognormal weights)."""
+    n, a, b = G.barabasi_albert(20000, 3, seed=21)
+    w = np.random.default_rng(22).lognormal(0.0, 0.5, len(a))
+    pos = f32(G.uniform_positions(n, 0.0, 1000.0, seed=23))
+    with make_layout(n, a, b, w, pos, "single", theta=1.2) as L:
+        assert L.info("heavy_nodes") > 0
+        L.iterate(400)
+        L.sync()
+        xy = L.positions()
+        ff = L.forces(xy)
+    with make_layout(n, a, b, w, xy, "double", theta=1.2) as L:
+        fd = L.forces(xy)
+    assert rel_err(ff, fd) <= 1e-4
