@@ -189,19 +189,17 @@ k_batch(int ngraphs, BatchGraph *graphs, const int *queue, int *next, int iterat
                         __syncthreads();
                         const int m = min(T, n - j0);
                         if (sizeof(R) == 4 && !adjust) {
-                            // the factor capped at FLT_MAX: a coincident
-                            // pair (d2 = 0, xd = yd = 0) adds 0, as the
-                            // reference's factor 0 for d2 = 0
-                            constexpr float BIG = 3.402823466e38f;
+                            // d2 carries 1e-30 (as k_exact): a coincident
+                            // pair (xd = yd = 0) has a finite factor, so it
+                            // adds 0, the reference's factor for d2 = 0
                             if (n <= T) { // one node per thread
 #pragma unroll 4
                                 for (int jj = 0; jj < m; jj++) {
                                     const R4 q = tile[jj];
                                     const float xda = (float) ma.x - (float) q.x;
                                     const float yda = (float) ma.y - (float) q.y;
-                                    const float d2a = fmaf(xda, xda, yda * yda);
-                                    const float ga =
-                                        fminf((float) q.z * __fdividef(1.0f, d2a), BIG);
+                                    const float d2a = fmaf(xda, xda, fmaf(yda, yda, 1e-30f));
+                                    const float ga = (float) q.z * __fdividef(1.0f, d2a);
                                     axa = (R) fmaf(xda, ga, (float) axa);
                                     aya = (R) fmaf(yda, ga, (float) aya);
                                 }
@@ -213,12 +211,10 @@ k_batch(int ngraphs, BatchGraph *graphs, const int *queue, int *next, int iterat
                                     const float yda = (float) ma.y - (float) q.y;
                                     const float xdb = (float) mb.x - (float) q.x;
                                     const float ydb = (float) mb.y - (float) q.y;
-                                    const float d2a = fmaf(xda, xda, yda * yda);
-                                    const float d2b = fmaf(xdb, xdb, ydb * ydb);
-                                    const float ga =
-                                        fminf((float) q.z * __fdividef(1.0f, d2a), BIG);
-                                    const float gb =
-                                        fminf((float) q.z * __fdividef(1.0f, d2b), BIG);
+                                    const float d2a = fmaf(xda, xda, fmaf(yda, yda, 1e-30f));
+                                    const float d2b = fmaf(xdb, xdb, fmaf(ydb, ydb, 1e-30f));
+                                    const float ga = (float) q.z * __fdividef(1.0f, d2a);
+                                    const float gb = (float) q.z * __fdividef(1.0f, d2b);
                                     axa = (R) fmaf(xda, ga, (float) axa);
                                     aya = (R) fmaf(yda, ga, (float) aya);
                                     axb = (R) fmaf(xdb, gb, (float) axb);

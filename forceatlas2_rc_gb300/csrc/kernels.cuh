@@ -1802,21 +1802,23 @@ k_exact(int n, R scaling, const typename RT<R>::R4 *__restrict__ nodes,
         const R4 *q = tile + b * TILE;
         const int cnt = min(TILE, j1 - j0 - t * TILE);
         if constexpr (sizeof(R) == 4 && !ADJUST) {
-            // FP32: 7 FP32-pipe operations, one min and one MUFU reciprocal
-            // per pair; the thread's scaling * m_i multiplies the sums once
-            // at the end. A coincident pair (xd = yd = 0, d2 = 0) has an
-            // infinite reciprocal: capping g at FLT_MAX makes its term 0,
-            // the reference's factor for d2 = 0. (d2 is also 0 when both
-            // offsets are below 1e-19, whose squares flush to zero; such a
-            // pair has no meaningful float force either way.)
+            // FP32: 7 FP32-pipe operations and one MUFU reciprocal per
+            // pair; the thread's scaling * m_i multiplies the sums once at
+            // the end. d2 carries 1e-30 (d2 = xd^2 + (yd^2 + 1e-30), one FMA
+            // each): a coincident pair (xd = yd = 0) then has a finite
+            // factor below 1e30 * m_j, so its term is 0 -- the reference's
+            // factor for d2 = 0 -- without a compare; any other pair of
+            // float positions is at least ~1e-14 apart in d2 for
+            // coordinates of 1e-3 or more, which the 1e-30 leaves unchanged
+            // to float precision.
 #pragma unroll 4
             for (int jj = 0; jj < cnt; jj++) {
                 const R4 p = q[jj];
 #pragma unroll
                 for (int u = 0; u < IPT; u++) {
                     const float xd = xi[u] - p.x, yd = yi[u] - p.y;
-                    const float d2 = fmaf(xd, xd, yd * yd);
-                    const float g = fminf(p.z * __fdividef(1.0f, d2), 3.402823466e38f);
+                    const float d2 = fmaf(xd, xd, fmaf(yd, yd, 1e-30f));
+                    const float g = p.z * __fdividef(1.0f, d2);
                     ax[u] = fmaf(xd, g, ax[u]);
                     ay[u] = fmaf(yd, g, ay[u]);
                 }
