@@ -488,14 +488,25 @@ template <bool CTA> __device__ __forceinline__ int arrive(int *v)
 
 // The climb of leaf k (sorted position) of an n-node tree: every region it
 // reaches second gets its sums (agg) and its traversal records.
-template <class R, bool CTA>
+//
+// LOCAL: the block's threads climb from the leaves [s0, s1) (256 P of them),
+// so both arrivals at a region whose range lies in [s0, s1) come from this
+// block: they count on a shared-memory counter (shv[r - s0]; a Karras region
+// r always lies in its own range) at CTA scope, whose release costs a CTA
+// fence instead of the device-scope fence of a global counter. Only the
+// regions that span two blocks' leaves count on visits[] at device scope.
+// The data a second arrival reads (the sibling's sums) was written by the
+// thread that arrived first, before its release; which scope the counter has
+// changes neither the order of the sums nor the tree.
+template <class R, bool CTA, bool LOCAL = false>
 __device__ __forceinline__ void climb(int k, int n, const typename RT<R>::R4 *psort,
                                       const int2 *child,
                                       const int *parent,
                                       const int2 *range,
                                       const int *rope, int *visits,
                                       Agg<R> *agg, typename RT<R>::R4 *rec_c, int2 *rec_t,
-                                      R wscale, int *status)
+                                      R wscale, int *status, int *shv = nullptr, int s0 = 0,
+                                      int s1 = 0)
 {
     const int nl = n - 1;
     int r = parent[nl + k];
@@ -503,6 +514,57 @@ __device__ __forceinline__ void climb(int k, int n, const typename RT<R>::R4 *ps
     // the sibling's are loaded
     int prev = nl + k;
     Agg<R> mine = leaf_agg(psort[k]);
+    if (LOCAL) {
+        // the links of the region above (children, range, parent) are
+        // loaded as soon as the region is known, before the arrival there
+        // and while the current region's sums are made: one L2 round trip
+        // a level less on the chain of the climb
+        int2 c = make_int2(-1, -1), rg = make_int2(-1, -1);
+        int up = -1;
+        if ((unsigned) r < (unsigned) nl) {
+            c = child[r];
+            rg = range[r];
+            up = parent[r];
+        }
+        for (int depth = 0; r >= 0; depth++) {
+            if (r >= nl || depth > 160) {
+                atomicOr(status + ST_ERROR, ERR_BOUNDS);
+                return;
+            }
+            const bool here =
+                rg.x >= s0 && rg.y < s1 && (unsigned) (r - s0) < (unsigned) (s1 - s0);
+            if ((here ? arrive<true>(shv + (r - s0)) : arrive<false>(visits + r)) == 0) return;
+            int2 cn = make_int2(-1, -1), rgn = make_int2(-1, -1);
+            int upn = -1;
+            if ((unsigned) up < (unsigned) nl) {
+                cn = child[up];
+                rgn = range[up];
+                upn = parent[up];
+            }
+            if (c.x < 0 || c.y < 0 || c.x >= nl + n || c.y >= nl + n || rg.x < 0 ||
+                rg.y < 0 || rg.y >= n || (c.x != prev && c.y != prev)) {
+                atomicOr(status + ST_ERROR, ERR_BOUNDS);
+                return;
+            }
+            const int2 links =
+                make_int2(rg.y - rg.x >= 8 ? c.x : bucket_pack(rg.x, rg.y), rope[rg.y]);
+            const bool from_a = c.x == prev;
+            const int other = from_a ? c.y : c.x;
+            const Agg<R> o =
+                other >= nl ? leaf_agg(psort[other - nl]) : load_agg_cg(agg + other);
+            const Agg<R> q = from_a ? agg_combine(mine, o) : agg_combine(o, mine);
+            agg[r] = q;
+            rec_c[r] = agg_record(q, wscale);
+            rec_t[r] = links;
+            mine = q;
+            prev = r;
+            r = up;
+            c = cn;
+            rg = rgn;
+            up = upn;
+        }
+        return;
+    }
     // a Karras tree over 32-bit keys and n < 2^27 nodes is < 64 levels deep
     for (int depth = 0; r >= 0; depth++) {
         if (r >= nl || depth > 160) {
@@ -545,22 +607,29 @@ k_aggregate(int n, const typename RT<R>::R4 *__restrict__ psort,
             typename RT<R>::R4 *__restrict__ rec_c, int2 *__restrict__ rec_t, R wscale,
             int *__restrict__ status)
 {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    __shared__ int shv[256];
+    shv[threadIdx.x] = 0;
+    __syncthreads();
+    const int s0 = blockIdx.x * 256, s1 = min(s0 + 256, n);
+    const int k = s0 + threadIdx.x;
     if (k < n)
-        climb<R, false>(k, n, psort, child, parent, range, rope, visits, agg, rec_c, rec_t,
-                        wscale, status);
+        climb<R, false, true>(k, n, psort, child, parent, range, rope, visits, agg, rec_c,
+                              rec_t, wscale, status, shv, s0, s1);
 }
 
 // The climbs of P leaves per thread, one after the other: with n/P threads
 // the launch fits in fewer waves of blocks (1M leaves one per thread are 3.2
 // waves of 2048 threads on 152 SMs), and a climb no longer waits for a later
 // wave to finish the region above it. CONTIG: thread t takes leaves tP ..
-// tP+P-1; else lane l of warp w takes leaves (wP+q)32+l, q < P. Which thread
-// computes a region does not change what it computes: the tree is the same.
-// In float the launch bound keeps 2048 threads per SM (32 registers), which
-// the choice of P (pick_climb) counts on.
+// tP+P-1; else lane l of warp w takes leaves (wP+q)32+l, q < P. Either way a
+// block takes the 256 P leaves from 256 P blockIdx.x on, whose inner regions
+// count their arrivals in shared memory. Which thread computes a region does
+// not change what it computes: the tree is the same. In float the launch
+// bound keeps 1536 threads per SM (40 registers: the early-loaded links of
+// the next level spill at 32), which the choice of P
+// (pick_climb) counts on.
 template <class R, int P, bool CONTIG>
-__global__ void __launch_bounds__(256, sizeof(R) == 4 ? 8 : 4)
+__global__ void __launch_bounds__(256, sizeof(R) == 4 ? 6 : 4)
 k_aggregate_multi(int n, const typename RT<R>::R4 *__restrict__ psort,
                   const int2 *__restrict__ child, const int *__restrict__ parent,
                   const int2 *__restrict__ range, const int *__restrict__ rope,
@@ -568,13 +637,18 @@ k_aggregate_multi(int n, const typename RT<R>::R4 *__restrict__ psort,
                   typename RT<R>::R4 *__restrict__ rec_c, int2 *__restrict__ rec_t, R wscale,
                   int *__restrict__ status)
 {
+    __shared__ int shv[256 * P];
+#pragma unroll
+    for (int q = 0; q < P; q++) shv[q * 256 + threadIdx.x] = 0;
+    __syncthreads();
+    const int s0 = blockIdx.x * (256 * P), s1 = min(s0 + 256 * P, n);
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
 #pragma unroll 1
     for (int q = 0; q < P; q++) {
         const int k = CONTIG ? t * P + q : ((t >> 5) * P + q) * 32 + (t & 31);
         if (k < n)
-            climb<R, false>(k, n, psort, child, parent, range, rope, visits, agg, rec_c, rec_t,
-                            wscale, status);
+            climb<R, false, true>(k, n, psort, child, parent, range, rope, visits, agg, rec_c,
+                                  rec_t, wscale, status, shv, s0, s1);
     }
 }
 

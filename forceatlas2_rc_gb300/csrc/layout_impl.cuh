@@ -74,8 +74,13 @@ template <class R> struct Layout : LayoutBase {
     bool block_sort = false; // few keys: the one-block sort
 
     // Leaves per thread of the tree's climb, from the ratio x of leaves to
-    // the threads the device holds at once (2048 per SM in float). Measured
-    // on a GB300 (FP32, SBM graphs, climb time in ms for 1 / 2 / 4 / 8
+    // the threads the device holds at once (1536 per SM in float, 40
+    // registers). With block-local arrivals and the links of the next level
+    // loaded early (gather + Karras + climb in ms for 1 / 2 / 4 / 8 leaves
+    // per thread): BA 1e5 (x 0.43) 0.052 / 0.054 / 0.057 / 0.070; SBM 3e5
+    // (x 1.3) 0.071 / 0.066 / 0.066 / 0.078; 1e6 (x 4.3) 0.141 / 0.126 /
+    // 0.148 / 0.144; 3e6 0.346 / 0.276 / 0.287 / 0.405. Earlier build (2048
+    // threads per SM, device-scope arrivals only; climb alone, 1 / 2 / 4 / 8
     // leaves per thread): 2e5 leaves (x 0.64) 0.069 / 0.074 / 0.084 / 0.123;
     // 4e5 (x 1.3) 0.101 / 0.091 / 0.100 / 0.142; 6e5 (x 1.9) 0.128 / 0.107 /
     // 0.117 / 0.155; 1e6 (x 3.2) 0.186 / 0.157 / 0.159 / 0.199; 2e6 (x 6.4)
