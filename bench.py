@@ -1164,7 +1164,7 @@ def main():
                          "batch: 4096 graphs in one persistent launch; "
                          "serve: the layout server on a Poisson job trace")
     ap.add_argument("--walk", default="deferred",
-                    choices=["warp", "thread", "wide", "pair", "quad", "deferred"],
+                    choices=list(WALKS),
                     help="Barnes-Hut walk (the same interactions; deferred is the "
                          "FP32 default)")
     args = ap.parse_args()
