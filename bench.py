@@ -984,9 +984,10 @@ def headline(args, local, ws, pg):
     stream = torch.cuda.ExternalStream(L.stream, device=local)
     # kernels of one captured iteration: Morton codes (with the sort's digit
     # histograms), 4 sort passes, gather + Karras tree, the bottom-up sums,
-    # the traversal, (the hubs' attraction, if any), attraction with the
-    # swing totals and the speed update, the displacement (with the next
-    # bounding box); no memset
+    # the traversal; beside the tree and the traversal on a second stream,
+    # (the hubs' attraction, if any) gravity and attraction; then the join
+    # with the swing totals and the speed update, the displacement (with the
+    # next bounding box); no memset
     launches = int(L.info("launches_per_iteration"))
 
     if args.profile_only:

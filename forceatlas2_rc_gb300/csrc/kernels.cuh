@@ -1207,7 +1207,11 @@ __device__ __forceinline__ Inc<float> load_inc(const Inc<float> *p)
 }
 __device__ __forceinline__ Inc<double> load_inc(const Inc<double> *p) { return *p; }
 
-template <class R, bool SKIP_HEAVY = false>
+//
+// OWN (FP32, the attraction run beside the walk): f is the attraction's own
+// buffer, and the sum starts at 0 -- at a hub's incidence sum, which
+// k_attract_heavy<R, true> wrote there.
+template <class R, bool SKIP_HEAVY = false, bool OWN = false>
 __device__ __forceinline__ void attract_one(int i, R gravity, int strong, int linlog, int adjust,
                                             const typename RT<R>::R2 *pos,
                                             const R *mass,
@@ -1218,8 +1222,12 @@ __device__ __forceinline__ void attract_one(int i, R gravity, int strong, int li
 {
     const typename RT<R>::R2 p = pos[i];
     const R xi = p.x, yi = p.y;
-    const typename RT<R>::R2 a = f[i];
-    R ax = a.x, ay = a.y;
+    R ax = R(0), ay = R(0);
+    if (!OWN || (SKIP_HEAVY && off[i + 1] - off[i] >= HEAVY_DEGREE)) {
+        const typename RT<R>::R2 a = f[i];
+        ax = a.x;
+        ay = a.y;
+    }
     if (gravity != R(0)) {
         const R dist = fsqrt(xi * xi + yi * yi);
         if (dist > R(0)) {
@@ -1293,7 +1301,9 @@ k_heavy_list(int n, const int *__restrict__ off, int *__restrict__ list, int cap
 // the lanes' sums are added pairwise across lane distances 16, 8, 4, 2, 1
 // (every lane ends with the same total). Gravity follows in the attraction
 // launch.
-template <class R>
+// SET (the attraction run beside the walk): the sum is written to f, the
+// attraction's own buffer, instead of added to the repulsion there.
+template <class R, bool SET = false>
 __global__ void __launch_bounds__(256)
 k_attract_heavy(int nheavy, const int *__restrict__ list, int linlog, int adjust,
                 const typename RT<R>::R2 *__restrict__ pos, const R *__restrict__ size,
@@ -1327,9 +1337,29 @@ k_attract_heavy(int nheavy, const int *__restrict__ list, int linlog, int adjust
         ay += __shfl_xor_sync(0xffffffffu, ay, o);
     }
     if (lane == 0) {
-        const typename RT<R>::R2 a = f[i];
-        f[i] = mk2<R>(a.x + ax, a.y + ay);
+        if (SET) {
+            f[i] = mk2<R>(ax, ay);
+        } else {
+            const typename RT<R>::R2 a = f[i];
+            f[i] = mk2<R>(a.x + ax, a.y + ay);
+        }
     }
+}
+
+// Gravity and attraction of every node into the attraction's own buffer fa
+// (FP32, run on a second stream beside the tree build and the walk):
+// grid-stride over the nodes with a grid of a few blocks per SM, so that
+// the walk keeps most of every SM. k_join_swing adds fa to the repulsion.
+template <class R>
+__global__ void __launch_bounds__(256)
+k_attract_own(int n, R gravity, int strong, int linlog, int adjust,
+              const typename RT<R>::R2 *__restrict__ pos, const R *__restrict__ mass,
+              const R *__restrict__ size, const int *__restrict__ off,
+              const Inc<R> *__restrict__ inc, typename RT<R>::R2 *__restrict__ fa)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        attract_one<R, true, true>(i, gravity, strong, linlog, adjust, pos, mass, size, off, inc,
+                                   fa);
 }
 
 // ---- 7. swinging, traction, FP64 totals and the speed update --------------
@@ -1603,6 +1633,39 @@ k_attract_swing(int n, R gravity, int strong, int linlog, int adjust,
         swing_node<R>(i, n, f, fold, mass, fixed, sw, tr, acc);
     }
     swing_finish<R>(acc, n, fixed, sw, tr, partial, ticket, st, status);
+}
+
+// The join of the attraction run beside the walk: a node's force is its
+// repulsion (f) plus its gravity and attraction (fa), then its swinging and
+// traction, and the totals with the speed update.
+template <class R>
+__global__ void __launch_bounds__(256)
+k_join_swing(int n, const typename RT<R>::R2 *__restrict__ fa, typename RT<R>::R2 *__restrict__ f,
+             const typename RT<R>::R2 *__restrict__ fold, const R *__restrict__ mass,
+             const uint8_t *__restrict__ fixed, R *__restrict__ sw, R *__restrict__ tr,
+             double2 *__restrict__ partial, unsigned *__restrict__ ticket,
+             SpeedState *__restrict__ st, int *__restrict__ status)
+{
+    SwingAcc<R> acc;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) {
+        const typename RT<R>::R2 r = f[i], a = fa[i];
+        f[i] = mk2<R>(r.x + a.x, r.y + a.y);
+        swing_node<R>(i, n, f, fold, mass, fixed, sw, tr, acc);
+    }
+    swing_finish<R>(acc, n, fixed, sw, tr, partial, ticket, st, status);
+}
+
+// f += fa (the forces of one evaluation, fa2cu_layout_forces, in the order
+// the iteration adds them).
+template <class R>
+__global__ void __launch_bounds__(256)
+k_add_forces(int n, const typename RT<R>::R2 *__restrict__ fa, typename RT<R>::R2 *__restrict__ f)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const typename RT<R>::R2 r = f[i], a = fa[i];
+    f[i] = mk2<R>(r.x + a.x, r.y + a.y);
 }
 
 // ---- 8. displacement (pipeline.cl:476-506) ---------------------------------

@@ -137,6 +137,13 @@ template <class R> struct Layout : LayoutBase {
     unsigned long long *counts = nullptr;
     cudaGraphExec_t g1 = nullptr, g8 = nullptr;
     cudaEvent_t ev[8] = {};
+    // FP32 Barnes-Hut: the attraction on a second stream beside the tree
+    // build and the walk, into its own buffer fatt, on attract_grid blocks
+    // per SM (beside())
+    int overlap = sizeof(R) == 4 ? 1 : 0, attract_grid = 1;
+    cudaStream_t s2 = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    R2 *fatt = nullptr;
 
     ~Layout() override
     {
@@ -146,6 +153,9 @@ template <class R> struct Layout : LayoutBase {
         for (auto &e : ev)
             if (e) cudaEventDestroy(e);
         mem.release();
+        if (ev_fork) cudaEventDestroy(ev_fork);
+        if (ev_join) cudaEventDestroy(ev_join);
+        if (s2) cudaStreamDestroy(s2);
         if (s) cudaStreamDestroy(s);
     }
 
@@ -195,6 +205,7 @@ template <class R> struct Layout : LayoutBase {
             agg = mem.get<Agg<R>>(nn - 1);
             rec_c = mem.get<R4>(nn - 1);
             rec_t = mem.get<int2>(nn - 1);
+            if (sizeof(R) == 4) fatt = mem.get<R2>(nn);
         } else {
             packed = mem.get<R4>(nn);
             if (exact_nrows > 1) exact_part = mem.get<R2>((size_t) exact_nrows * nn);
@@ -293,6 +304,14 @@ template <class R> struct Layout : LayoutBase {
             FA2_TRY(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking),
                     "could not create a CUDA stream", 1);
         for (auto &e : ev) FA2_TRY(cudaEventCreate(&e), "could not create a CUDA event", 1);
+        if (sizeof(R) == 4 && rep == FA2CU_REPULSION_BH) {
+            FA2_TRY(cudaStreamCreateWithFlags(&s2, cudaStreamNonBlocking),
+                    "could not create a CUDA stream", 1);
+            FA2_TRY(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming),
+                    "could not create a CUDA event", 1);
+            FA2_TRY(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming),
+                    "could not create a CUDA event", 1);
+        }
 
         mem.pool = opts ? opts->pool : nullptr;
         mem.s = s;
@@ -581,10 +600,59 @@ template <class R> struct Layout : LayoutBase {
     void launch_forces()
     {
         launch_repel();
-        launch_attraction();
+        if (beside()) { // the iteration's order: repulsion + (gravity + attraction)
+            launch_attraction_own(s);
+            k_add_forces<R><<<ceil_div(n, 256), 256, 0, s>>>(n, fatt, f);
+        } else {
+            launch_attraction();
+        }
+    }
+    // FP32 Barnes-Hut: gravity and attraction into fatt, on stream s2
+    // beside the tree build and the walk, added to the repulsion by the
+    // join (overlap 1: forked after the sort; 2: after the tree; 0: the
+    // attraction fused with the totals after the walk). Forked after the
+    // sort on one block per SM it measured 0.727 -> 0.711 ms an iteration at
+    // 10^6 SBM nodes, 0.229 -> 0.209 ms at 10^5 BA nodes; forked before the
+    // sort it delays the sort's tiles (0.77-0.85 ms, whatever the stream
+    // priorities), and more blocks per SM slow the walk.
+    bool beside() const { return overlap && s2 && fatt && !serial_totals<R>(n); }
+    void launch_attraction_own(cudaStream_t st)
+    {
+        if constexpr (sizeof(R) == 4) {
+            int sms = 0;
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+            if (nheavy > 0)
+                k_attract_heavy<R, true><<<ceil_div(nheavy, 8), 256, 0, st>>>(
+                    nheavy, heavy, linlog, adjust, pos, size, inc_off, inc, fatt);
+            const int grid =
+                std::max(1, std::min(std::max(sms, 1) * attract_grid, ceil_div(n, 256)));
+            k_attract_own<R><<<grid, 256, 0, st>>>(n, gravity, strong, linlog, adjust, pos, mass,
+                                                   size, inc_off, inc, fatt);
+        }
+    }
+    void launch_join_swing()
+    {
+        k_join_swing<R><<<ceil_div(n, 256), 256, 0, s>>>(
+            n, fatt, f, fold, mass, fixed, sw, trac, swing_partial,
+            (unsigned *) (status + ST_TICKET_SWING), st, status);
     }
     void launch_iteration()
     {
+        if (beside()) {
+            launch_build();
+            launch_sort();
+            if (overlap == 2) launch_tree();
+            cudaEventRecord(ev_fork, s);
+            cudaStreamWaitEvent(s2, ev_fork, 0);
+            launch_attraction_own(s2);
+            cudaEventRecord(ev_join, s2);
+            if (overlap != 2) launch_tree();
+            launch_repulsion();
+            cudaStreamWaitEvent(s, ev_join, 0);
+            launch_join_swing();
+            launch_move();
+            return;
+        }
         launch_repel();
         launch_attraction_swing();
         launch_move();
@@ -725,7 +793,12 @@ template <class R> struct Layout : LayoutBase {
             }
             launch_repulsion();
             cudaEventRecord(ev[e++], s);
-            launch_attraction_swing(); // "attraction": with the totals and speed
+            if (beside()) { // "attraction": run after the walk here, then the join
+                launch_attraction_own(s);
+                launch_join_swing();
+            } else {
+                launch_attraction_swing(); // with the totals and speed
+            }
             cudaEventRecord(ev[e++], s);
             launch_move();
             cudaEventRecord(ev[e++], s);
@@ -797,6 +870,18 @@ template <class R> struct Layout : LayoutBase {
     {
         if (!strcmp(name, "sort_threads") && (value == 256 || value == 512 || value == 1024)) {
             ss.tile_threads = (int) value;
+            return recapture();
+        }
+        if (!strcmp(name, "overlap") && (value == 0 || value == 1 || value == 2)) {
+            if (value != 0 && !s2) {
+                set_message("the attraction runs beside the walk in FP32 Barnes-Hut layouts only");
+                return 1;
+            }
+            overlap = (int) value;
+            return recapture();
+        }
+        if (!strcmp(name, "attract_grid") && value >= 1 && value <= 8) {
+            attract_grid = (int) value;
             return recapture();
         }
         if (!strcmp(name, "sort_block") && (value == 0 || value == 1)) {

@@ -96,7 +96,15 @@ int fa2cu_layout_traversal_counts(fa2cu_layout *L, double counts[2]);
  *   "sort_block"   1: the one-block sort (at most 4096 nodes; default there),
  *                  0: the tiled sort;
  *   "keep_traction" 1: keep each node's traction of the last iteration for
- *                  fa2cu_layout_swing (n more reals on the device). */
+ *                  fa2cu_layout_swing (n more reals on the device);
+ *   "overlap"      single precision, Barnes-Hut: 1 gravity and attraction
+ *                  computed on a second stream beside the tree build and
+ *                  the walk (forked after the sort; default), into a buffer
+ *                  of their own that is then added to the repulsion; 2 the
+ *                  same forked after the tree build; 0 the attraction after
+ *                  the walk, added to the repulsion node by node (forces
+ *                  equal to ~1e-7);
+ *   "attract_grid" blocks per SM of that attraction, 1 (default) to 8. */
 int fa2cu_layout_option(fa2cu_layout *L, const char *name, double value);
 
 /* A figure of the layout, by name: "launches_per_iteration" (kernels of one

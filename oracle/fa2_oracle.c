@@ -892,11 +892,13 @@ static void repulse_mixed(const pipe_ws_f *w, const pipe_ws_d *wd,
     free(pairs);
 }
 
-/* Its attraction: as attract_core_f, except that a node of at least
- * ORC_HEAVY incidences gets its attraction first, as 32 interleaved partial
- * sums (incidence e to partial e mod 32, each in edge order) added pairwise
- * across distances 16, 8, 4, 2, 1 -- a warp's sum on the device -- then its
- * gravity. */
+/* Its gravity and attraction, summed apart from the repulsion (the device
+ * computes them beside the walk) and then added to it: from 0, the
+ * gravity, then the incidences in edge order; a node of at least ORC_HEAVY
+ * incidences starts from its attraction, as 32 interleaved partial sums
+ * (incidence e to partial e mod 32, each in edge order) added pairwise
+ * across distances 16, 8, 4, 2, 1 -- a warp's sum on the device -- and
+ * adds its gravity. */
 #define ORC_HEAVY 128
 static void attract_mixed(int n, float gravity, int strong, int linlog,
                           int adjust, const float *p, const float *mass,
@@ -907,8 +909,8 @@ static void attract_mixed(int n, float gravity, int strong, int linlog,
         const float xi = p[2 * i], yi = p[2 * i + 1];
         const float si = adjust ? size[i] : 0.0f;
         const int heavy = off[i + 1] - off[i] >= ORC_HEAVY;
+        float lx[32], ly[32];
         if (heavy) {
-            float lx[32], ly[32];
             for (int l = 0; l < 32; l++) {
                 lx[l] = ly[l] = 0.0f;
                 for (int e = off[i] + l; e < off[i + 1]; e += 32) {
@@ -934,10 +936,8 @@ static void attract_mixed(int n, float gravity, int strong, int linlog,
                 memcpy(lx, tx, sizeof(lx));
                 memcpy(ly, ty, sizeof(ly));
             }
-            f[2 * i] += lx[0];
-            f[2 * i + 1] += ly[0];
         }
-        float ax = f[2 * i], ay = f[2 * i + 1];
+        float ax = heavy ? lx[0] : 0.0f, ay = heavy ? ly[0] : 0.0f;
         if (gravity != 0.0f) {
             const float dist = sqrtf(xi * xi + yi * yi);
             if (dist > 0.0f) {
@@ -961,8 +961,8 @@ static void attract_mixed(int n, float gravity, int strong, int linlog,
                 ay += yd * g;
             }
         }
-        f[2 * i] = ax;
-        f[2 * i + 1] = ay;
+        f[2 * i] += ax;
+        f[2 * i + 1] += ay;
     }
 }
 

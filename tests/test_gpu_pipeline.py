@@ -436,7 +436,8 @@ def test_heavy_nodes_single(gpu, orc, opts):
     summed by a warp each, in a fixed order that the oracle's restatement of
     the FP32 path mirrors: forces within 1e-5 of it, and within 1e-4 of the
     FP64 forces (2e-3 with prevent_overlap); the hub kernel is one more
-    launch per iteration."""
+    launch per iteration (and the attraction beside the walk, with its
+    join, one more than the attraction fused with the totals)."""
     n, a, b = G.barabasi_albert(6000, 3, seed=12)
     rng = np.random.default_rng(13)
     hub_a = np.concatenate([np.zeros(3000, np.int32), np.ones(700, np.int32)])
@@ -452,12 +453,15 @@ def test_heavy_nodes_single(gpu, orc, opts):
         f = L.forces(pos)
         heavy = L.info("heavy_nodes")
         launches = L.info("launches_per_iteration")
+        L.option("overlap", 0)
+        launches_fused = L.info("launches_per_iteration")
     with make_layout(n, a, b, w, pos, "double", size=size, theta=1.2, **opts) as L:
         fd = L.forces(pos)
         launches_d = L.info("launches_per_iteration")
     deg = np.diff(go.inc_off)
     assert heavy == (deg >= 128).sum() > 2
-    assert launches == launches_d + 1
+    assert launches_fused == launches_d + 1
+    assert launches == launches_fused + 1
     assert rel_err(f, orc.pipe_forces(p, pos, "m")) <= 1e-5
     assert rel_err(f, fd) <= (2e-3 if opts.get("adjust") else 1e-4)
 
@@ -480,3 +484,54 @@ def test_fp32_forces_near_equilibrium_with_hubs(gpu):
     with make_layout(n, a, b, w, xy, "double", theta=1.2) as L:
         fd = L.forces(xy)
     assert rel_err(ff, fd) <= 1e-4
+
+
+@pytest.mark.parametrize("opts", [dict(), dict(linlog=True, outbound=True),
+                                  dict(adjust=True, linlog=True)])
+def test_attraction_beside_the_walk(gpu, orc, opts):
+    """FP32 Barnes-Hut: gravity and attraction run on a second stream beside
+    the tree build and the walk, into a buffer of their own, added to the
+    repulsion by the join. Where the branch forks (after the sort or after
+    the tree) and how many blocks it has change no bit of the trajectory;
+    the force query gives the iteration's forces (the oracle's FP32 mirror
+    within 1e-5; 5e-3 with prevent_overlap, whose near-contact force is
+    ill-conditioned in float); the attraction fused after the walk
+    (overlap 0) sums in
+    another order: forces within 1e-6, positions after one iteration within
+    1e-6 of the layout's extent. Hubs (the warp-summed attraction) included."""
+    n, a, b = G.barabasi_albert(20000, 3, seed=31)
+    rng = np.random.default_rng(32)
+    a = np.concatenate([a, np.zeros(400, np.int32)])
+    b = np.concatenate([b, rng.choice(np.arange(1, n), 400, replace=False).astype(np.int32)])
+    w = rng.lognormal(0.0, 0.5, len(a))
+    pos = f32(G.uniform_positions(n, 0, 1000, seed=33))
+    adjust = opts.get("adjust", False)
+    size = f32(rng.uniform(0.5, 3.0, n)) if adjust else None
+    kw = {k: v for k, v in opts.items() if k != "outbound"}
+    go = orc.prepare_large(n, a, b, w, outbound=opts.get("outbound", False))
+    p, keep = orc.full_params(go, size=size, theta=1.2, **kw)
+    runs = {}
+    for name, ov, grid in (("after_sort", 1, 1), ("after_tree", 2, 1), ("grid4", 1, 4),
+                           ("fused", 0, 1)):
+        with make_layout(n, a, b, w, pos, "single", size=size, theta=1.2,
+                         outbound=opts.get("outbound", False), **kw) as L:
+            assert L.info("heavy_nodes") > 0
+            L.option("overlap", ov)
+            L.option("attract_grid", grid)
+            f = L.forces(pos)
+            L.iterate(1)
+            L.sync()
+            xy1 = L.positions()
+            L.iterate(9)
+            L.sync()
+            runs[name] = (f, xy1, L.positions(), L.speed())
+    base = runs["after_sort"]
+    for name in ("after_tree", "grid4"):
+        for k in range(3):
+            np.testing.assert_array_equal(runs[name][k], base[k], err_msg=name)
+        assert runs[name][3] == base[3]
+    assert rel_err(base[0], orc.pipe_forces(p, pos, "m")) <= (5e-3 if adjust else 1e-5)
+    fused = runs["fused"]
+    assert rel_err(fused[0], base[0]) <= 1e-6
+    ext = np.abs(base[1]).max()
+    assert np.abs(fused[1] - base[1]).max() <= 1e-6 * ext
