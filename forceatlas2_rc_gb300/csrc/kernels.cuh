@@ -1637,7 +1637,8 @@ k_attract_swing(int n, R gravity, int strong, int linlog, int adjust,
 
 // The join of the attraction run beside the walk: a node's force is its
 // repulsion (f) plus its gravity and attraction (fa), then its swinging and
-// traction, and the totals with the speed update.
+// traction, and the totals with the speed update. Grid-stride over a few
+// blocks per SM: few block partials for the last block to add up.
 template <class R>
 __global__ void __launch_bounds__(256)
 k_join_swing(int n, const typename RT<R>::R2 *__restrict__ fa, typename RT<R>::R2 *__restrict__ f,
@@ -1647,8 +1648,7 @@ k_join_swing(int n, const typename RT<R>::R2 *__restrict__ fa, typename RT<R>::R
              SpeedState *__restrict__ st, int *__restrict__ status)
 {
     SwingAcc<R> acc;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const typename RT<R>::R2 r = f[i], a = fa[i];
         f[i] = mk2<R>(r.x + a.x, r.y + a.y);
         swing_node<R>(i, n, f, fold, mass, fixed, sw, tr, acc);

@@ -141,6 +141,10 @@ template <class R> struct Layout : LayoutBase {
     // build and the walk, into its own buffer fatt, on attract_grid blocks
     // per SM (beside())
     int overlap = sizeof(R) == 4 ? 1 : 0, attract_grid = 1;
+    // grid of the join: 4 blocks per SM, grid-stride (0.709-0.712 -> 0.703
+    // ms an iteration at 10^6 SBM nodes against one block per 256 nodes,
+    // whose last block added 3907 partials)
+    int join_blocks = 152 * 4;
     cudaStream_t s2 = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     R2 *fatt = nullptr;
@@ -632,7 +636,7 @@ template <class R> struct Layout : LayoutBase {
     }
     void launch_join_swing()
     {
-        k_join_swing<R><<<ceil_div(n, 256), 256, 0, s>>>(
+        k_join_swing<R><<<std::min(ceil_div(n, 256), join_blocks), 256, 0, s>>>(
             n, fatt, f, fold, mass, fixed, sw, trac, swing_partial,
             (unsigned *) (status + ST_TICKET_SWING), st, status);
     }
@@ -878,6 +882,10 @@ template <class R> struct Layout : LayoutBase {
                 return 1;
             }
             overlap = (int) value;
+            return recapture();
+        }
+        if (!strcmp(name, "join_blocks") && value >= 1 && value <= 1 << 20) {
+            join_blocks = (int) value;
             return recapture();
         }
         if (!strcmp(name, "attract_grid") && value >= 1 && value <= 8) {

@@ -104,7 +104,10 @@ int fa2cu_layout_traversal_counts(fa2cu_layout *L, double counts[2]);
  *                  same forked after the tree build; 0 the attraction after
  *                  the walk, added to the repulsion node by node (forces
  *                  equal to ~1e-7);
- *   "attract_grid" blocks per SM of that attraction, 1 (default) to 8. */
+ *   "attract_grid" blocks per SM of that attraction, 1 (default) to 8;
+ *   "join_blocks"  blocks of 256 threads of the join that adds it to the
+ *                  repulsion and sums the swing totals (default 608: few
+ *                  block partials for its last block). */
 int fa2cu_layout_option(fa2cu_layout *L, const char *name, double value);
 
 /* A figure of the layout, by name: "launches_per_iteration" (kernels of one
