@@ -1436,6 +1436,34 @@ template <class R> struct SwingAcc {
 template <class R>
 __device__ __forceinline__ void swing_node(int i, int n, const typename RT<R>::R2 *f,
                                            const typename RT<R>::R2 *fold, const R *mass,
+                                           const uint8_t *fixed, R *sw, R *tr, SwingAcc<R> &acc);
+
+// The same from the node's force a, its previous force b and mass m, loaded
+// by the caller.
+template <class R>
+__device__ __forceinline__ void swing_node_v(int i, typename RT<R>::R2 a, typename RT<R>::R2 b,
+                                             R m, const uint8_t *fixed, R *sw, R *tr,
+                                             SwingAcc<R> &acc)
+{
+    const R sx = b.x - a.x, sy = b.y - a.y;
+    const R tx = b.x + a.x, ty = b.y + a.y;
+    const R s = m * fsqrt(sx * sx + sy * sy);
+    const R t = R(0.5) * m * fsqrt(tx * tx + ty * ty);
+    sw[i] = s;
+    if (tr) tr[i] = t; // kept for the serial totals, or on request
+    if (fixed && fixed[i]) return;
+    if constexpr (sizeof(R) == 4) {
+        acc.s = ff_add(acc.s, ff_from((float) s));
+        acc.t = ff_add(acc.t, ff_from((float) t));
+    } else {
+        acc.ds = __dadd_rn(acc.ds, (double) s);
+        acc.dt = __dadd_rn(acc.dt, (double) t);
+    }
+}
+
+template <class R>
+__device__ __forceinline__ void swing_node(int i, int n, const typename RT<R>::R2 *f,
+                                           const typename RT<R>::R2 *fold, const R *mass,
                                            const uint8_t *fixed, R *sw, R *tr, SwingAcc<R> &acc)
 {
     const typename RT<R>::R2 a = f[i], b = fold[i];
@@ -1647,11 +1675,33 @@ k_join_swing(int n, const typename RT<R>::R2 *__restrict__ fa, typename RT<R>::R
              double2 *__restrict__ partial, unsigned *__restrict__ ticket,
              SpeedState *__restrict__ st, int *__restrict__ status)
 {
+    typedef typename RT<R>::R2 R2;
     SwingAcc<R> acc;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const typename RT<R>::R2 r = f[i], a = fa[i];
-        f[i] = mk2<R>(r.x + a.x, r.y + a.y);
-        swing_node<R>(i, n, f, fold, mass, fixed, sw, tr, acc);
+    // U nodes a round, their loads issued together; the nodes of a thread
+    // are added to its sums in node order
+    constexpr int U = 4;
+    const int stride = gridDim.x * blockDim.x;
+    for (int i0 = blockIdx.x * blockDim.x + threadIdx.x; i0 < n; i0 += U * stride) {
+        R2 r[U], a[U], b[U];
+        R m[U];
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            const int i = i0 + u * stride;
+            if (i < n) {
+                r[u] = f[i];
+                a[u] = fa[i];
+                b[u] = fold[i];
+                m[u] = mass[i];
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            const int i = i0 + u * stride;
+            if (i >= n) break;
+            const R2 t = mk2<R>(r[u].x + a[u].x, r[u].y + a[u].y);
+            f[i] = t;
+            swing_node_v<R>(i, t, b[u], m[u], fixed, sw, tr, acc);
+        }
     }
     swing_finish<R>(acc, n, fixed, sw, tr, partial, ticket, st, status);
 }
