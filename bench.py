@@ -1136,6 +1136,10 @@ def headline(args, local, ws, pg):
         "force_err_fp32_vs_fp64_start": _rel_err(f0_32, f0_64),
         "iterations_per_s": 1000.0 * args.steps / ms,
         "phase_ms": ph,
+        "phase_note": ("CUDA events around each phase, its kernels run one after the "
+                       "other; in the captured iteration the attraction runs beside the "
+                       "climb and the traversal, so the phases add up to more than "
+                       "ms_per_step"),
         "gpu_launches": launches * args.steps, "launches_per_iteration": launches,
         "e2e": e2e, "roofline": roofline, "cpu_baseline": None,
         "clocks": clocks,

@@ -605,7 +605,7 @@ template <class R> struct Layout : LayoutBase {
     {
         launch_repel();
         if (beside()) { // the iteration's order: repulsion + (gravity + attraction)
-            launch_attraction_own(s);
+            launch_attraction_own(s, true);
             k_add_forces<R><<<ceil_div(n, 256), 256, 0, s>>>(n, fatt, f);
         } else {
             launch_attraction();
@@ -620,7 +620,9 @@ template <class R> struct Layout : LayoutBase {
     // sort it delays the sort's tiles (0.77-0.85 ms, whatever the stream
     // priorities), and more blocks per SM slow the walk.
     bool beside() const { return overlap && s2 && fatt && !serial_totals<R>(n); }
-    void launch_attraction_own(cudaStream_t st)
+    // alone: nothing runs beside it (the force query, the phase times), one
+    // thread per node; else attract_grid blocks per SM
+    void launch_attraction_own(cudaStream_t st, bool alone)
     {
         if constexpr (sizeof(R) == 4) {
             int sms = 0;
@@ -629,7 +631,8 @@ template <class R> struct Layout : LayoutBase {
                 k_attract_heavy<R, true><<<ceil_div(nheavy, 8), 256, 0, st>>>(
                     nheavy, heavy, linlog, adjust, pos, size, inc_off, inc, fatt);
             const int grid =
-                std::max(1, std::min(std::max(sms, 1) * attract_grid, ceil_div(n, 256)));
+                alone ? ceil_div(n, 256)
+                      : std::max(1, std::min(std::max(sms, 1) * attract_grid, ceil_div(n, 256)));
             k_attract_own<R><<<grid, 256, 0, st>>>(n, gravity, strong, linlog, adjust, pos, mass,
                                                    size, inc_off, inc, fatt);
         }
@@ -648,7 +651,7 @@ template <class R> struct Layout : LayoutBase {
             if (overlap == 2) launch_tree();
             cudaEventRecord(ev_fork, s);
             cudaStreamWaitEvent(s2, ev_fork, 0);
-            launch_attraction_own(s2);
+            launch_attraction_own(s2, false);
             cudaEventRecord(ev_join, s2);
             if (overlap != 2) launch_tree();
             launch_repulsion();
@@ -797,8 +800,8 @@ template <class R> struct Layout : LayoutBase {
             }
             launch_repulsion();
             cudaEventRecord(ev[e++], s);
-            if (beside()) { // "attraction": run after the walk here, then the join
-                launch_attraction_own(s);
+            if (beside()) { // "attraction": here after the walk, one thread per node, and the join
+                launch_attraction_own(s, true);
                 launch_join_swing();
             } else {
                 launch_attraction_swing(); // with the totals and speed
