@@ -854,6 +854,8 @@ walk_deferred(int k, int n, R scaling, R theta2, double theta2d,
     typedef typename RT<R>::R4 R4;
     const R4 me = psort[k];
     const R xi = me.x, yi = me.y, mi = me.z, si = me.w;
+    // a far region's pull is (scaling m_i) m / d^2
+    const R smi = scaling * mi;
     R ax = R(0), ay = R(0), cx = R(0), cy = R(0);
     const bool comp = COMP && sizeof(R) == 4 && mi >= R(HUB_MASS);
     const int nl = n - 1;
@@ -861,17 +863,20 @@ walk_deferred(int k, int n, R scaling, R theta2, double theta2d,
     int q[DEFER_QUEUE];
     int nq = 0;
     int cur = 0;
-    // one step per region (n - 1) and per single node reached as a leaf (n)
-    const int cap = 2 * n + 64;
-    for (int step = 0;; step++) {
-        // the end of the walk (-1), or a link out of range
-        if ((unsigned) cur >= nend || step > cap) {
-            if (cur != -1) atomicOr(status + ST_ERROR, ERR_BOUNDS);
-            break;
-        }
+    // one step per region (n - 1) and per single node reached as a leaf
+    // (n): at most 2n + 65 steps
+    int budget = 2 * n + 65;
+    for (;;) {
+        // one test a step for the rare cases: a single node, the end of the
+        // walk (-1), a link out of range, the step budget spent
+        --budget;
         int bucket;
-        if (cur >= nl) { // a single node
-            const int j = cur - nl;
+        if (((unsigned) cur >= (unsigned) nl) | (budget < 0)) {
+            if ((unsigned) cur >= nend || budget < 0) {
+                if (cur != -1) atomicOr(status + ST_ERROR, ERR_BOUNDS);
+                break;
+            }
+            const int j = cur - nl; // a single node
             bucket = bucket_pack(j, j);
             cur = rope[j];
         } else {
@@ -882,7 +887,7 @@ walk_deferred(int k, int n, R scaling, R theta2, double theta2d,
             const bool far =
                 region_far(d2, c.w, theta2, agg + cur, (float) xi, (float) yi, theta2d);
             if (far) {
-                const R g = fdiv(scaling * (mi * c.z), d2);
+                const R g = fdiv(smi * c.z, d2);
                 acc_add(ax, cx, xd * g, comp);
                 acc_add(ay, cy, yd * g, comp);
                 cur = t.y;

@@ -837,6 +837,7 @@ static void repulse_mixed(const pipe_ws_f *w, const pipe_ws_d *wd,
     for (int k = 0; k < n; k++) {
         const float xi = ps[4 * k], yi = ps[4 * k + 1];
         const float mi = ps[4 * k + 2], si = ps[4 * k + 3];
+        const float smi = scaling * mi; /* a far region's pull: smi m / d^2 */
         float ax = 0.0f, ay = 0.0f;
         int np = 0; /* queued ranges (first, last) */
         int stack[160];
@@ -858,7 +859,7 @@ static void repulse_mixed(const pipe_ws_f *w, const pipe_ws_d *wd,
                     far = (ex * ex + ey * ey) * theta2d > wd->ni[4 * r + 3];
                 }
                 if (far) {
-                    const float g = scaling * (mi * ni[4 * r + 2]) / d2;
+                    const float g = smi * ni[4 * r + 2] / d2;
                     ax += xd * g;
                     ay += yd * g;
                     continue;
