@@ -827,6 +827,10 @@ __device__ __forceinline__ void acc_add(float &s, float &c, float v, bool comp)
 }
 __device__ __forceinline__ void acc_add(double &s, double &, double v, bool) { s += v; }
 
+// Read-only loads of the walk's inputs (non-coherent path in float).
+__device__ __forceinline__ float4 ldg_r4(const float4 *p) { return __ldg(p); }
+__device__ __forceinline__ double4_32a ldg_r4(const double4_32a *p) { return *p; }
+
 template <class R, bool ADJUST>
 __device__ __forceinline__ void sum_pairs(int k, const int *q, int nq, R xi, R yi, R mi, R si,
                                           R scaling, const typename RT<R>::R4 *psort, R &ax,
@@ -836,7 +840,7 @@ __device__ __forceinline__ void sum_pairs(int k, const int *q, int nq, R xi, R y
         const int last = bucket_last(q[b]);
         for (int j = bucket_first(q[b]); j <= last; j++) {
             if (j == k) continue;
-            const typename RT<R>::R4 p = psort[j];
+            const typename RT<R>::R4 p = ldg_r4(psort + j);
             const R xd = xi - p.x, yd = yi - p.y;
             const R g = rep_factor<R, ADJUST>(xd * xd + yd * yd, mi * p.z, si + p.w, scaling);
             acc_add(ax, cx, xd * g, comp);
@@ -878,10 +882,10 @@ walk_deferred(int k, int n, R scaling, R theta2, double theta2d,
             }
             const int j = cur - nl; // a single node
             bucket = bucket_pack(j, j);
-            cur = rope[j];
+            cur = __ldg(rope + j);
         } else {
-            const R4 c = rec_c[cur];
-            const int2 t = rec_t[cur];
+            const R4 c = ldg_r4(rec_c + cur);
+            const int2 t = __ldg(rec_t + cur);
             const R xd = xi - c.x, yd = yi - c.y;
             const R d2 = xd * xd + yd * yd;
             const bool far =
