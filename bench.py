@@ -742,6 +742,7 @@ def batch_result(args, local, work, full=False):
         "value": value, "unit": "layouts/s", "steps": steps, "ms_per_step": ms / steps,
         "graphs": count, "nodes": nodes, "iterations": iters,
         "exact_below": tuned["exact_below"], "threads": tuned["threads"],
+        "nodes_per_thread": tuned["nodes_per_thread"],
         "node_iters_per_s": nodes * iters * steps / (ms / 1000.0),
         "e2e": {"value": count / e2e_s, "unit": "layouts/s",
                 "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),

@@ -72,7 +72,8 @@ def load(build_if_missing: bool = False):
                                                  C.c_void_p, C.c_void_p]),
         "fa2cu_noalloc_status": (C.c_int, [C.c_void_p]),
         "fa2cu_batch_open": (C.c_void_p, [C.POINTER(FullParams), C.c_int,
-                                          C.POINTER(P_D), C.c_int, C.c_int]),
+                                          C.POINTER(P_D), C.c_int, C.c_int,
+                                          C.c_int]),
         "fa2cu_batch_iterate": (C.c_int, [C.c_void_p, C.c_int]),
         "fa2cu_batch_sync": (C.c_int, [C.c_void_p]),
         "fa2cu_batch_positions": (C.c_int, [C.c_void_p, C.c_int, P_D]),
@@ -81,7 +82,7 @@ def load(build_if_missing: bool = False):
         "fa2cu_batch_phase_cycles": (C.c_int, [C.c_void_p, C.c_int, P_D]),
         "fa2cu_batch_bytes": (C.c_double, [C.c_void_p]),
         "fa2cu_batch_close": (None, [C.c_void_p]),
-        "fa2cu_batch_tune": (C.c_int, [C.c_int, C.c_int, P_I, P_I]),
+        "fa2cu_batch_tune": (C.c_int, [C.c_int, C.c_int, P_I, P_I, P_I]),
         "fa2cu_server_open": (C.c_void_p, [C.POINTER(ServerConfig)]),
         "fa2cu_server_submit": (C.c_longlong, [C.c_void_p, C.POINTER(FullParams),
                                                P_D, C.c_int]),

@@ -23,14 +23,15 @@ from .layout import Graph, _cols, _params
 
 def tune(device: int = 0, precision: str = "single") -> dict:
     """The autotuner's choice on this device: ``exact_below`` (graphs with
-    fewer nodes use the all-pairs repulsion) and ``threads`` per block.
-    Measured once per device and precision, then cached."""
+    fewer nodes use the all-pairs repulsion), ``threads`` per block and
+    ``nodes_per_thread`` of the all-pairs sum (its tile shape). Measured once
+    per device and precision, then cached."""
     lib = _lib.load()
-    eb, th = C.c_int(0), C.c_int(0)
+    eb, th, npt = C.c_int(0), C.c_int(0), C.c_int(0)
     if lib.fa2cu_batch_tune(int(device), int(precision == "double"),
-                            C.byref(eb), C.byref(th)) != 0:
+                            C.byref(eb), C.byref(th), C.byref(npt)) != 0:
         raise RuntimeError(_lib.error())
-    return dict(exact_below=eb.value, threads=th.value)
+    return dict(exact_below=eb.value, threads=th.value, nodes_per_thread=npt.value)
 
 
 class Batch:
@@ -41,7 +42,7 @@ class Batch:
     ``Layout`` (scaling, gravity, theta, jitter_tolerance, strong, linlog,
     adjust, size, fixed) for every graph; ``per_graph`` (a list of dicts, one
     per graph) overrides them graph by graph. ``exact_below`` / ``threads``
-    default to the autotuner's values.
+    / ``nodes_per_thread`` default to the autotuner's values.
     """
 
     _KEYS = ("size", "fixed", "scaling", "gravity", "theta", "jitter_tolerance",
@@ -49,7 +50,8 @@ class Batch:
 
     def __init__(self, graphs: list, pos: list, *, precision: str = "single",
                  device: int = 0, exact_below: int | None = None,
-                 threads: int | None = None, per_graph: list | None = None,
+                 threads: int | None = None, nodes_per_thread: int | None = None,
+                 per_graph: list | None = None,
                  **settings):
         bad = set(settings) - set(self._KEYS)
         if bad:
@@ -86,7 +88,8 @@ class Batch:
         ptrs = (P_D * count)(*[dptr(a) for a in xy])
         self.h = self.lib.fa2cu_batch_open(
             arr, count, ptrs, -1 if exact_below is None else int(exact_below),
-            0 if threads is None else int(threads))
+            0 if threads is None else int(threads),
+            0 if nodes_per_thread is None else int(nodes_per_thread))
         if not self.h:
             raise RuntimeError(_lib.error())
 

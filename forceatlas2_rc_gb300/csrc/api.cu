@@ -366,9 +366,11 @@ void fa2cu_layout_close(fa2cu_layout *L)
 
 // ---- batched layouts ---------------------------------------------------------
 
-static int tuned[64][2][2]; // [device][double] -> exact_below, threads (0: not yet)
+// [device][double] -> exact_below, threads, nodes per thread (0: not yet)
+static int tuned[64][2][3];
 
-int fa2cu_batch_tune(int device, int use_double, int *exact_below, int *threads)
+int fa2cu_batch_tune(int device, int use_double, int *exact_below, int *threads,
+                     int *nodes_per_thread)
 {
     if (check_device(device)) return 1;
     if (device >= 64) {
@@ -377,20 +379,21 @@ int fa2cu_batch_tune(int device, int use_double, int *exact_below, int *threads)
     }
     int *t = tuned[device][use_double ? 1 : 0];
     if (!t[1]) {
-        const int rc = use_double ? tune_batch_f64(device, &t[0], &t[1])
-                                  : tune_batch_f32(device, &t[0], &t[1]);
+        const int rc = use_double ? tune_batch_f64(device, &t[0], &t[1], &t[2])
+                                  : tune_batch_f32(device, &t[0], &t[1], &t[2]);
         if (rc) {
-            t[0] = t[1] = 0;
+            t[0] = t[1] = t[2] = 0;
             return 1;
         }
     }
     *exact_below = t[0];
     *threads = t[1];
+    if (nodes_per_thread) *nodes_per_thread = t[2];
     return 0;
 }
 
 fa2cu_batch *fa2cu_batch_open(const fa2_full_params *graphs, int count, const double *const *pos,
-                              int exact_below, int threads)
+                              int exact_below, int threads, int nodes_per_thread)
 {
     if (!graphs || !pos || count < 1) {
         set_message("invalid arguments: a batch needs at least one graph");
@@ -422,14 +425,20 @@ fa2cu_batch *fa2cu_batch_open(const fa2_full_params *graphs, int count, const do
         set_message("threads must be 256 or 512 (0: tuned)");
         return nullptr;
     }
-    if (exact_below < 0 || threads == 0) {
-        int eb = 0, th = 0;
-        if (fa2cu_batch_tune(dev, dbl, &eb, &th)) return nullptr;
+    if (nodes_per_thread != 0 && nodes_per_thread != 1 && nodes_per_thread != 2) {
+        set_message("nodes_per_thread must be 1 or 2 (0: tuned)");
+        return nullptr;
+    }
+    if (exact_below < 0 || threads == 0 || nodes_per_thread == 0) {
+        int eb = 0, th = 0, np = 0;
+        if (fa2cu_batch_tune(dev, dbl, &eb, &th, &np)) return nullptr;
         if (exact_below < 0) exact_below = eb;
         if (threads == 0) threads = th;
+        if (nodes_per_thread == 0) nodes_per_thread = np;
     }
-    BatchBase *impl = dbl ? make_batch_f64(graphs, count, pos, exact_below, threads)
-                          : make_batch_f32(graphs, count, pos, exact_below, threads);
+    BatchBase *impl =
+        dbl ? make_batch_f64(graphs, count, pos, exact_below, threads, nodes_per_thread)
+            : make_batch_f32(graphs, count, pos, exact_below, threads, nodes_per_thread);
     if (!impl) return nullptr;
     fa2cu_batch *B = new fa2cu_batch;
     B->impl = impl;

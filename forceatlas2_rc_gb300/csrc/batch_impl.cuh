@@ -101,7 +101,7 @@ template <int W> __device__ double block_sum(double v, double *scratch)
 template <class R, int T>
 __global__ void __launch_bounds__(T, (sizeof(R) == 8 ? 512 : 1024) / T)
 k_batch(int ngraphs, BatchGraph *graphs, const int *queue, int *next, int iterations,
-        BatchArrays<R> A, int *status)
+        BatchArrays<R> A, int npt, int *status)
 {
     typedef typename RT<R>::R2 R2;
     typedef typename RT<R>::R4 R4;
@@ -174,10 +174,12 @@ k_batch(int ngraphs, BatchGraph *graphs, const int *queue, int *next, int iterat
                     psort[i] = mk4<R>(p.x, p.y, mass[i], adjust ? size[i] : R(0));
                 }
                 R4 *tile = reinterpret_cast<R4 *>(&cnt[0][0]);
-                // two nodes per thread (i and i + T): each tile record feeds
-                // two independent sums; every node still sums j ascending
-                for (int i0 = 0; i0 < n; i0 += 2 * T) {
-                    const int ia = i0 + tid, ib = ia + T;
+                // the tile shape (autotuned): npt = 2 nodes per thread (i
+                // and i + T), each tile record feeding two independent sums,
+                // or 1; every node sums j ascending either way
+                const bool two = npt == 2 && n > T;
+                for (int i0 = 0; i0 < n; i0 += two ? 2 * T : T) {
+                    const int ia = i0 + tid, ib = two ? ia + T : n;
                     const R4 zero = mk4<R>(R(0), R(0), R(0), R(0));
                     const R4 ma = ia < n ? psort[ia] : zero, mb = ib < n ? psort[ib] : zero;
                     R axa = R(0), aya = R(0), axb = R(0), ayb = R(0);
@@ -192,7 +194,7 @@ k_batch(int ngraphs, BatchGraph *graphs, const int *queue, int *next, int iterat
                             // d2 carries 1e-30 (as k_exact): a coincident
                             // pair (xd = yd = 0) has a finite factor, so it
                             // adds 0, the reference's factor for d2 = 0
-                            if (n <= T) { // one node per thread
+                            if (!two) { // one node per thread
 #pragma unroll 4
                                 for (int jj = 0; jj < m; jj++) {
                                     const R4 q = tile[jj];
@@ -434,7 +436,7 @@ k_batch(int ngraphs, BatchGraph *graphs, const int *queue, int *next, int iterat
 template <class R> struct Batch : BatchBase {
     typedef typename RT<R>::R2 R2;
     typedef typename RT<R>::R4 R4;
-    int G = 0, N = 0, E = 0, threads = 512;
+    int G = 0, N = 0, E = 0, threads = 512, npt = 2;
     cudaStream_t s = nullptr;
     DevMem mem;
     BatchArrays<R> A{};
@@ -457,10 +459,11 @@ template <class R> struct Batch : BatchBase {
     int count() const override { return G; }
 
     int open(const fa2_full_params *ps, int count, const double *const *pos, int exact_below,
-             int nthreads)
+             int nthreads, int nodes_per_thread)
     {
         G = count;
         threads = nthreads;
+        npt = nodes_per_thread;
         node0.resize(G);
         nsize.resize(G);
         bool any_adjust = false, any_fixed = false;
@@ -608,9 +611,11 @@ template <class R> struct Batch : BatchBase {
     {
         cudaMemsetAsync(next, 0, sizeof(int), s);
         if (threads == 256)
-            k_batch<R, 256><<<blocks, 256, 0, s>>>(G, graphs, queue, next, iterations, A, status);
+            k_batch<R, 256><<<blocks, 256, 0, s>>>(G, graphs, queue, next, iterations, A, npt,
+                                                   status);
         else
-            k_batch<R, 512><<<blocks, 512, 0, s>>>(G, graphs, queue, next, iterations, A, status);
+            k_batch<R, 512><<<blocks, 512, 0, s>>>(G, graphs, queue, next, iterations, A, npt,
+                                                   status);
     }
 
     // The work-counter reset and the persistent launch, captured once per
@@ -664,10 +669,10 @@ template <class R> struct Batch : BatchBase {
         if (!rc) {
             if (threads == 256)
                 k_batch<R, 256><<<blocks, 256, 0, s>>>(G, graphs, queue, next, iterations, P,
-                                                       status);
+                                                       npt, status);
             else
                 k_batch<R, 512><<<blocks, 512, 0, s>>>(G, graphs, queue, next, iterations, P,
-                                                       status);
+                                                       npt, status);
         }
         std::vector<unsigned long long> h((size_t) blocks * 8);
         if (!rc)
@@ -742,13 +747,13 @@ template <class R> struct Batch : BatchBase {
 
 template <class R>
 BatchBase *make_batch(const fa2_full_params *ps, int count, const double *const *pos,
-                      int exact_below, int threads)
+                      int exact_below, int threads, int npt)
 {
     const int dev = ps[0].device;
     FA2_TRY(cudaSetDevice(dev), "could not use the CUDA device", nullptr);
     Batch<R> *B = new Batch<R>();
     B->device = dev;
-    if (B->open(ps, count, pos, exact_below, threads)) {
+    if (B->open(ps, count, pos, exact_below, threads, npt)) {
         delete B;
         return nullptr;
     }
@@ -756,12 +761,14 @@ BatchBase *make_batch(const fa2_full_params *ps, int count, const double *const 
 }
 
 // ---- autotuner -------------------------------------------------------------------
-// The exact-vs-Barnes-Hut crossover and the block size, measured on the
-// device: Erdos-Renyi graphs (mean degree 8), two per SM, laid out for 2
-// iterations (after 2) in each mode, at 64, 128, .. 16384 nodes until the
-// tree is faster, then at quarter-octave sizes below that one; the crossover
-// is the smallest size measured at which the tree is faster. Block sizes 256
-// and 512 are compared on 2048-node graphs.
+// The exact-vs-Barnes-Hut crossover, the block size and the exact sum's tile
+// shape, measured on the device: Erdos-Renyi graphs (mean degree 8), two per
+// SM, laid out for 2 iterations (after 2) in each mode, at 64, 128, .. 16384
+// nodes until the tree is faster, then at quarter-octave sizes below that
+// one; the crossover is the smallest size measured at which the tree is
+// faster. Block sizes 256 and 512 are compared on 2048-node graphs; then 1
+// or 2 nodes per thread of the exact sum on graphs of 3/4 of the crossover
+// (at least one block of nodes more).
 
 struct TuneGraphs {
     std::vector<std::vector<int>> off, node;
@@ -836,9 +843,10 @@ static void tune_graphs(TuneGraphs &t, int n, int copies, int device, int use_do
 
 // Milliseconds per graph-iteration of a batch of these graphs (-1 on error).
 template <class R>
-static double time_batch(TuneGraphs &t, int exact_below, int threads)
+static double time_batch(TuneGraphs &t, int exact_below, int threads, int npt = 2)
 {
-    BatchBase *B = make_batch<R>(t.ps.data(), (int) t.ps.size(), t.pp.data(), exact_below, threads);
+    BatchBase *B =
+        make_batch<R>(t.ps.data(), (int) t.ps.size(), t.pp.data(), exact_below, threads, npt);
     if (!B) return -1.0;
     double ms = -1.0;
     cudaEvent_t e0, e1;
@@ -861,7 +869,7 @@ static double time_batch(TuneGraphs &t, int exact_below, int threads)
     return ms;
 }
 
-template <class R> int tune_batch(int device, int *exact_below, int *threads)
+template <class R> int tune_batch(int device, int *exact_below, int *threads, int *npt)
 {
     int sms = 0;
     FA2_TRY(cudaSetDevice(device), "could not use the CUDA device", 1);
@@ -903,8 +911,15 @@ template <class R> int tune_batch(int device, int *exact_below, int *threads)
     tune_graphs(t, 2048, copies, device, sizeof(R) == 8);
     const double t256 = time_batch<R>(t, 0, 256), t512 = time_batch<R>(t, 0, 512);
     if (t256 < 0 || t512 < 0) return 1;
+    const int th = t256 < t512 ? 256 : 512;
+    TuneGraphs u;
+    tune_graphs(u, std::min(std::max(cross * 3 / 4, th + 1), 4096), copies, device,
+                sizeof(R) == 8);
+    const double t1 = time_batch<R>(u, 1 << 30, th, 1), t2 = time_batch<R>(u, 1 << 30, th, 2);
+    if (t1 < 0 || t2 < 0) return 1;
     *exact_below = cross;
-    *threads = t256 < t512 ? 256 : 512;
+    *threads = th;
+    *npt = t1 < t2 ? 1 : 2;
     return 0;
 }
 

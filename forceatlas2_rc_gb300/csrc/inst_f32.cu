@@ -20,12 +20,12 @@ RepulseBase *make_repulse_f32(int device, int n, int adjust, int bh)
     return make_repulse<float>(device, n, adjust, bh);
 }
 BatchBase *make_batch_f32(const fa2_full_params *ps, int count, const double *const *pos,
-                          int exact_below, int threads)
+                          int exact_below, int threads, int npt)
 {
-    return make_batch<float>(ps, count, pos, exact_below, threads);
+    return make_batch<float>(ps, count, pos, exact_below, threads, npt);
 }
-int tune_batch_f32(int device, int *exact_below, int *threads)
+int tune_batch_f32(int device, int *exact_below, int *threads, int *npt)
 {
-    return tune_batch<float>(device, exact_below, threads);
+    return tune_batch<float>(device, exact_below, threads, npt);
 }
 } // namespace fa2cu

@@ -88,14 +88,16 @@ struct BatchBase {
 };
 
 // NULL on failure (message set). exact_below: graphs of fewer nodes use the
-// exact repulsion; threads: block size (256 or 512).
+// exact repulsion; threads: block size (256 or 512); npt: nodes per thread
+// of the exact sum (1 or 2).
 BatchBase *make_batch_f32(const fa2_full_params *ps, int count, const double *const *pos,
-                          int exact_below, int threads);
+                          int exact_below, int threads, int npt);
 BatchBase *make_batch_f64(const fa2_full_params *ps, int count, const double *const *pos,
-                          int exact_below, int threads);
-// Crossover and block size measured on this device (0 on success).
-int tune_batch_f32(int device, int *exact_below, int *threads);
-int tune_batch_f64(int device, int *exact_below, int *threads);
+                          int exact_below, int threads, int npt);
+// Crossover, block size and tile shape measured on this device (0 on
+// success).
+int tune_batch_f32(int device, int *exact_below, int *threads, int *npt);
+int tune_batch_f64(int device, int *exact_below, int *threads, int *npt);
 
 // Host-side checks of caller data that the kernels index with: 0 if valid,
 // otherwise 1 with the message set.

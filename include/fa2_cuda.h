@@ -170,12 +170,15 @@ typedef struct fa2cu_batch fa2cu_batch;
  * positions (x then y). Device and precision are those of graphs[0].
  * Graphs with fewer than exact_below nodes use the exact repulsion, the others
  * Barnes-Hut over their own Morton/Karras tree; threads is the block size
- * (256 or 512). exact_below < 0 or threads == 0: the values measured by
- * fa2cu_batch_tune on this device. A graph's result does not depend on the
- * other graphs of the batch. NULL on error. */
+ * (256 or 512); nodes_per_thread (1 or 2) the tile shape of the exact sum
+ * (each thread sums that many nodes against the block's tile of `threads`
+ * records in shared memory). exact_below < 0, threads == 0 or
+ * nodes_per_thread == 0: the values measured by fa2cu_batch_tune on this
+ * device. A graph's result does not depend on the other graphs of the batch
+ * (nor on the tile shape). NULL on error. */
 fa2cu_batch *fa2cu_batch_open(const fa2_full_params *graphs, int count,
                               const double *const *pos, int exact_below,
-                              int threads);
+                              int threads, int nodes_per_thread);
 /* Enqueue `iterations` iterations of every graph (one launch). */
 int fa2cu_batch_iterate(fa2cu_batch *B, int iterations);
 int fa2cu_batch_sync(fa2cu_batch *B);
@@ -193,12 +196,13 @@ int fa2cu_batch_phase_cycles(fa2cu_batch *B, int iterations, double cycles[8]);
 double fa2cu_batch_bytes(const fa2cu_batch *B);
 void fa2cu_batch_close(fa2cu_batch *B);
 
-/* The autotuner: exact-vs-Barnes-Hut crossover (in nodes) and block size of
- * the batched engine, measured on `device` in the given precision (timed
- * batches of Erdos-Renyi graphs of 64 to 16384 nodes). Cached per device and
- * precision for the process. */
+/* The autotuner: exact-vs-Barnes-Hut crossover (in nodes), block size and
+ * the exact sum's nodes per thread of the batched engine, measured on
+ * `device` in the given precision (timed batches of Erdos-Renyi graphs of 64
+ * to 16384 nodes). Cached per device and precision for the process.
+ * nodes_per_thread may be NULL. */
 int fa2cu_batch_tune(int device, int use_double, int *exact_below,
-                     int *threads);
+                     int *threads, int *nodes_per_thread);
 
 /* ---- serving ------------------------------------------------------------ */
 

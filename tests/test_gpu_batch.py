@@ -187,14 +187,38 @@ def test_batch_tune_and_errors(gpu):
         t = tune(0, prec)
         assert t["threads"] in (256, 512)
         assert 64 <= t["exact_below"] <= 32768
+        assert t["nodes_per_thread"] in (1, 2)
         assert tune(0, prec) == t
     g, pos = case(100, 1)
     with pytest.raises(RuntimeError, match="threads"):
         Batch([g], [pos], threads=100)
+    with pytest.raises(RuntimeError, match="nodes_per_thread"):
+        Batch([g], [pos], nodes_per_thread=3)
     bad = Graph(100, [0], [1], [1.0])
     bad.inc_node = np.array([500, 0], np.int32)  # a neighbour out of range
     with pytest.raises(RuntimeError):
         Batch([g, bad], [pos, pos])
+
+
+@pytest.mark.parametrize("prec", ["single", "double"])
+@pytest.mark.parametrize("adjust", [False, True])
+def test_batch_exact_tile_shape(gpu, prec, adjust):
+    """The exact sum's tile shape (1 or 2 nodes per thread against the
+    block's tile of records) changes no bit of a graph's layout: every node
+    sums its pairs in ascending order either way. Graphs larger than a block
+    of nodes, so that the two-node shape is taken."""
+    cases = [case(n, 40 + n % 7) for n in (300, 700, 1500)]
+    gs, ps = [c[0] for c in cases], [c[1] for c in cases]
+    out = {}
+    for npt in (1, 2):
+        per = [dict(size=np.full(g.n, 1.5)) for g in gs] if adjust else None
+        with Batch(gs, ps, precision=prec, exact_below=1 << 20, threads=256,
+                   nodes_per_thread=npt, adjust=adjust, per_graph=per) as B:
+            B.iterate(4)
+            B.sync()
+            out[npt] = [B.positions(i) for i in range(len(gs))]
+    for a, b in zip(out[1], out[2]):
+        np.testing.assert_array_equal(a, b)
 
 
 def test_batch_matches_oracle(gpu, orc):
