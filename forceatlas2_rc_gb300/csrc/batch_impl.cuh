@@ -49,7 +49,9 @@ struct BatchGraph {
     int err, pad;
 };
 
-enum { BF_STRONG = 1, BF_LINLOG = 2, BF_ADJUST = 4, BF_FIXED = 8 };
+// BF_HUBS: a node of mass HUB_MASS or more (FP32: the walk compensates its
+// sums)
+enum { BF_STRONG = 1, BF_LINLOG = 2, BF_ADJUST = 4, BF_FIXED = 8, BF_HUBS = 16 };
 
 template <class R> struct BatchArrays {
     typedef typename RT<R>::R2 R2;
@@ -129,6 +131,7 @@ k_batch(int ngraphs, BatchGraph *graphs, const int *queue, int *next, int iterat
         const int flags = G->flags;
         const bool strong = flags & BF_STRONG, linlog = flags & BF_LINLOG;
         const bool adjust = flags & BF_ADJUST, anyfix = flags & BF_FIXED;
+        const bool hubs = flags & BF_HUBS;
         const R scaling = (R) G->scaling, gravity = (R) G->gravity;
         const double theta2d = G->theta2d;
         const R theta2 = (R) theta2d;
@@ -329,12 +332,32 @@ k_batch(int ngraphs, BatchGraph *graphs, const int *queue, int *next, int iterat
                 }
                 __syncthreads();
                 phase(BP_SUMS);
+                // FP32: the walk with its node pairs deferred (the single
+                // layout's), compensated for hubs; FP64: the per-thread walk
+                // in the reference's order
                 for (int k = tid; k < n; k += T) {
-                    const R2 fk =
-                        adjust ? walk<R, true>(k, n, scaling, theta2, theta2d, psort, rec_c,
-                                               rec_t, agg, rope, status)
-                               : walk<R, false>(k, n, scaling, theta2, theta2d, psort, rec_c,
-                                                rec_t, agg, rope, status);
+                    R2 fk;
+                    if constexpr (sizeof(R) == 4) {
+                        if (hubs)
+                            fk = adjust ? walk_deferred<R, true, true>(k, n, scaling, theta2,
+                                                                       theta2d, psort, rec_c,
+                                                                       rec_t, agg, rope, status)
+                                        : walk_deferred<R, false, true>(k, n, scaling, theta2,
+                                                                        theta2d, psort, rec_c,
+                                                                        rec_t, agg, rope, status);
+                        else
+                            fk = adjust ? walk_deferred<R, true>(k, n, scaling, theta2, theta2d,
+                                                                 psort, rec_c, rec_t, agg, rope,
+                                                                 status)
+                                        : walk_deferred<R, false>(k, n, scaling, theta2, theta2d,
+                                                                  psort, rec_c, rec_t, agg, rope,
+                                                                  status);
+                    } else {
+                        fk = adjust ? walk<R, true>(k, n, scaling, theta2, theta2d, psort, rec_c,
+                                                    rec_t, agg, rope, status)
+                                    : walk<R, false>(k, n, scaling, theta2, theta2d, psort, rec_c,
+                                                     rec_t, agg, rope, status);
+                    }
                     f[idx[k]] = fk;
                 }
             }
@@ -552,6 +575,11 @@ template <class R> struct Batch : BatchBase {
             if (p.linlog) fl |= BF_LINLOG;
             if (p.adjust) fl |= BF_ADJUST;
             if (gfixed[g]) fl |= BF_FIXED;
+            for (int i = 0; i < n; i++)
+                if ((float) p.mass[i] >= HUB_MASS) {
+                    fl |= BF_HUBS;
+                    break;
+                }
             q.flags = fl;
             q.scaling = p.scaling;
             q.gravity = p.gravity;
