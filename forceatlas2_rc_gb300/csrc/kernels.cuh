@@ -836,15 +836,23 @@ __device__ __forceinline__ void sum_pairs(int k, const int *q, int nq, R xi, R y
                                           R scaling, const typename RT<R>::R4 *psort, R &ax,
                                           R &ay, R &cx, R &cy, bool comp)
 {
-    for (int b = 0; b < nq; b++) {
-        const int last = bucket_last(q[b]);
-        for (int j = bucket_first(q[b]); j <= last; j++) {
-            if (j == k) continue;
+    // one loop over all the queued pairs (bucket after bucket, each in
+    // sorted order): the lanes of a warp run as many iterations as the
+    // lane with the most pairs, not the most nodes of each bucket in turn
+    if (nq <= 0) return;
+    int b = 0, j = bucket_first(q[0]), last = bucket_last(q[0]);
+    for (;;) {
+        if (j != k) {
             const typename RT<R>::R4 p = ldg_r4(psort + j);
             const R xd = xi - p.x, yd = yi - p.y;
             const R g = rep_factor<R, ADJUST>(xd * xd + yd * yd, mi * p.z, si + p.w, scaling);
             acc_add(ax, cx, xd * g, comp);
             acc_add(ay, cy, yd * g, comp);
+        }
+        if (++j > last) {
+            if (++b >= nq) break;
+            j = bucket_first(q[b]);
+            last = bucket_last(q[b]);
         }
     }
 }
