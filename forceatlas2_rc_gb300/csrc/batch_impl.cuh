@@ -97,11 +97,14 @@ template <int W> __device__ double block_sum(double v, double *scratch)
 
 // ---- the persistent kernel -----------------------------------------------------
 
-// FP32: two blocks of 512 (four of 256) threads per SM, 64 registers a
-// thread, which keeps 32 warps resident to hide the latency of the walk's
-// dependent loads. FP64 needs more registers: half as many blocks.
+// FP32: three blocks of 512 (six of 256) threads per SM, 40 registers a
+// thread (~120 bytes of spills, in the sort and tree phases): 48 warps
+// resident for the walk, which is bound by instruction issue. Against two
+// blocks of 512 at 63 registers: 7.30 -> 6.49 ms a batch iteration of 4096
+// graphs; four blocks (32 registers, ~400 bytes of spills) 6.60-6.70 ms.
+// FP64 needs more registers: one block of 512 (two of 256).
 template <class R, int T>
-__global__ void __launch_bounds__(T, (sizeof(R) == 8 ? 512 : 1024) / T)
+__global__ void __launch_bounds__(T, (sizeof(R) == 8 ? 512 : 1536) / T)
 k_batch(int ngraphs, BatchGraph *graphs, const int *queue, int *next, int iterations,
         BatchArrays<R> A, int npt, int *status)
 {
