@@ -67,8 +67,10 @@ TRAVERSE_L2_BYTES_PER_PAIR = 16
 # DRAM bytes (read + write) of one traversal launch on this workload
 # (dram__bytes_read.sum + dram__bytes_write.sum, one ncu capture of each
 # walk), and the share of cycles the schedulers issued (the kernel's bound)
-TRAVERSE_DRAM_BYTES = {"deferred": 51.79e6 + 2.92e6, "thread": 45.94e6 + 0.86e6}
-TRAVERSE_ISSUE_ACTIVE = {"deferred": 0.788, "thread": 0.805}
+TRAVERSE_DRAM_BYTES = {"deferred": 53.06e6 + 4.54e6, "thread": 45.94e6 + 0.86e6}
+TRAVERSE_ISSUE_ACTIVE = {"deferred": 0.757, "thread": 0.805}
+# and its L1 throughput (share of peak, same captures)
+TRAVERSE_L1_THROUGHPUT = {"deferred": 0.859, "thread": 0.78}
 
 
 def make_workload(small: bool = False):
@@ -1105,8 +1107,10 @@ def headline(args, local, ws, pg):
                 "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"],
                 "traffic": TRAVERSE_DRAM_BYTES.get(args.walk) if n == 1_000_000 else None,
                 "issue_active": TRAVERSE_ISSUE_ACTIVE.get(args.walk),
-                "bound_note": "issue- and L1-bound (ncu: issue active ~81 %, L1 throughput "
-                              "~76 %, 96 % L1 hits); the HBM fraction is small by design",
+                "l1_throughput": TRAVERSE_L1_THROUGHPUT.get(args.walk),
+                "bound_note": "L1- and issue-bound (ncu: L1 throughput ~86 % of peak, issue "
+                              "active ~76 %, 95 % L1 hits); the HBM fraction is small by "
+                              "design",
                 "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of "
                                   "one traversal launch on this workload",
                 "kernel": {"warp": "k_traverse_warp<float, 0>",
