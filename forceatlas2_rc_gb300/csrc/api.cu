@@ -8,6 +8,7 @@
 #include <stdio.h>
 #include <string.h>
 #include <time.h>
+#include <mutex>
 #include <vector>
 
 #include "session.h"
@@ -366,8 +367,10 @@ void fa2cu_layout_close(fa2cu_layout *L)
 
 // ---- batched layouts ---------------------------------------------------------
 
-// [device][double] -> exact_below, threads, nodes per thread (0: not yet)
+// [device][double] -> exact_below, threads, nodes per thread (0: not yet);
+// one tuning at a time (callers on several host threads wait for it)
 static int tuned[64][2][3];
+static std::mutex tune_lock;
 
 int fa2cu_batch_tune(int device, int use_double, int *exact_below, int *threads,
                      int *nodes_per_thread)
@@ -377,6 +380,7 @@ int fa2cu_batch_tune(int device, int use_double, int *exact_below, int *threads,
         set_message("the autotuner supports devices 0 to 63");
         return 1;
     }
+    std::lock_guard<std::mutex> hold(tune_lock);
     int *t = tuned[device][use_double ? 1 : 0];
     if (!t[1]) {
         const int rc = use_double ? tune_batch_f64(device, &t[0], &t[1], &t[2])
