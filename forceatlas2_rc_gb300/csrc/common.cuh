@@ -37,6 +37,33 @@ enum {
     WALK_DEFERRED = 5,
 };
 
+// Programmatic dependent launch. A kernel of the iteration may be launched
+// with the programmatic stream serialisation attribute (launch_k): its
+// blocks are then scheduled as its predecessor on the stream finishes,
+// without a launch gap. It calls pdl_wait before touching memory: the wait
+// returns once the predecessor grid has completed and its writes are
+// visible (at once for a kernel launched without the attribute). No kernel
+// triggers its dependents early, so a waiting block never holds an SM its
+// predecessor still needs.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_k(bool pdl, void (*kernel)(KArgs...), dim3 grid, dim3 block,
+                            size_t smem, cudaStream_t s, Args... args)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = pdl ? attr : nullptr;
+    cfg.numAttrs = pdl ? 1 : 0;
+    return cudaLaunchKernelEx(&cfg, kernel, ((KArgs) args)...);
+}
+
 // Nanoseconds of the GPU's global timer (bounds of every device-side wait).
 __device__ __forceinline__ unsigned long long global_ns()
 {

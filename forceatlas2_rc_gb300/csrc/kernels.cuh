@@ -264,6 +264,7 @@ k_morton(int n, const typename RT<R>::R2 *__restrict__ pos, const double *__rest
          uint32_t *__restrict__ lookback, size_t nlookback)
 {
     __shared__ SortHistShared H;
+    pdl_wait();
     if (aux) hist_begin(H, lookback, nlookback); // (uniform)
     const double minx = quant[0], miny = quant[1], scale = quant[2];
     float4 qf = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -310,6 +311,7 @@ k_gather_karras(int n, int adjust, const uint32_t *__restrict__ order,
                 int2 *__restrict__ range, int *__restrict__ parent, int *__restrict__ rope,
                 int *__restrict__ visits, int *__restrict__ status)
 {
+    pdl_wait();
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
     // the node's record is loaded first, so that its scattered loads are in
@@ -609,6 +611,7 @@ k_aggregate(int n, const typename RT<R>::R4 *__restrict__ psort,
 {
     __shared__ int shv[256];
     shv[threadIdx.x] = 0;
+    pdl_wait();
     __syncthreads();
     const int s0 = blockIdx.x * 256, s1 = min(s0 + 256, n);
     const int k = s0 + threadIdx.x;
@@ -640,6 +643,7 @@ k_aggregate_multi(int n, const typename RT<R>::R4 *__restrict__ psort,
     __shared__ int shv[256 * P];
 #pragma unroll
     for (int q = 0; q < P; q++) shv[q * 256 + threadIdx.x] = 0;
+    pdl_wait();
     __syncthreads();
     const int s0 = blockIdx.x * (256 * P), s1 = min(s0 + 256 * P, n);
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -939,6 +943,7 @@ k_traverse_deferred(int n, R scaling, R theta2, double theta2d,
                     const uint32_t *__restrict__ order, typename RT<R>::R2 *__restrict__ f,
                     int *__restrict__ status)
 {
+    pdl_wait();
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
     f[order[k]] = walk_deferred<R, ADJUST, COMP>(k, n, scaling, theta2, theta2d, psort, rec_c,
@@ -1753,6 +1758,7 @@ k_apply(int n, int adjust, const typename RT<R>::R2 *__restrict__ f,
         R *__restrict__ partial, R *__restrict__ bbox, double *__restrict__ quant,
         unsigned *__restrict__ ticket)
 {
+    pdl_wait();
     const bool stopped = status[ST_ERROR] != 0;
     const R speed = (R) st->speed;
     R mnx = (R) INFINITY, mny = (R) INFINITY, mxx = -(R) INFINITY, mxy = -(R) INFINITY;

@@ -145,6 +145,11 @@ template <class R> struct Layout : LayoutBase {
     // ms an iteration at 10^6 SBM nodes against one block per 256 nodes,
     // whose last block added 3907 partials)
     int join_blocks = 152 * 4;
+    // the iteration's kernels on the main stream launched as programmatic
+    // dependents (launch_k; option "pdl"), below 500,000 nodes: ms an
+    // iteration without / with, SBM 10^4 0.1431 / 0.1415, BA 10^5 0.2028 /
+    // 0.2004, SBM 10^6 0.6799 / 0.6855 (positions identical)
+    bool pdl = false;
     cudaStream_t s2 = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     R2 *fatt = nullptr;
@@ -328,6 +333,8 @@ template <class R> struct Layout : LayoutBase {
             // 3e5 0.054 / 0.054 / 0.066; 1e6 0.092 / 0.077 / 0.070; 3e6
             // 0.178 / 0.164 / 0.163
             ss.tile_threads = n < 600000 ? 512 : 1024;
+            pdl = n < 500000;
+            ss.pdl = pdl;
             block_sort = n <= SORT_BLOCK_MAX;
         }
         if (rep == FA2CU_REPULSION_EXACT) {
@@ -442,8 +449,8 @@ template <class R> struct Layout : LayoutBase {
         // the histograms, done counter and tickets start at zero: cleared at
         // open, then left at zero by the Morton kernel's last block for the
         // next sort (no memset in the iteration)
-        k_morton<R><<<nb, 256, 0, s>>>(n, pos, quant, key, order, ss.digit_total, ss.counts,
-                                       sort_status_words(n, 4));
+        launch_k(pdl, k_morton<R>, dim3(nb), dim3(256), 0, s, n, pos, quant, key, order,
+                 ss.digit_total, ss.counts, sort_status_words(n, 4));
     }
     void launch_sort()
     {
@@ -454,13 +461,13 @@ template <class R> struct Layout : LayoutBase {
     }
     void launch_tree()
     {
-        k_gather_karras<R><<<ceil_div(n, 256), 256, 0, s>>>(n, adjust, order, pos, mass, size,
-                                                            psort, key, child, range, parent,
-                                                            rope, visits, status);
+        launch_k(pdl, k_gather_karras<R>, dim3(ceil_div(n, 256)), dim3(256), 0, s, n, adjust,
+                 order, pos, mass, size, psort, key, child, range, parent, rope, visits, status);
         switch (climb_mode) {
         case 2:
-            k_aggregate_multi<R, 2, true><<<ceil_div(n, 512), 256, 0, s>>>(
-                n, psort, child, parent, range, rope, visits, agg, rec_c, rec_t, wscale, status);
+            launch_k(pdl, k_aggregate_multi<R, 2, true>, dim3(ceil_div(n, 512)), dim3(256), 0, s,
+                     n, psort, child, parent, range, rope, visits, agg, rec_c, rec_t, wscale,
+                     status);
             break;
         case 4:
             k_aggregate_multi<R, 4, true><<<ceil_div(n, 1024), 256, 0, s>>>(
@@ -523,9 +530,9 @@ template <class R> struct Layout : LayoutBase {
                             <<<g, 256, 0, s>>>(n, scaling, theta2, theta2d, psort, rec_c, rec_t,
                                                agg, rope, order, f, status);
                     else
-                        k_traverse_deferred<R, false, sizeof(R) == 4 ? 8 : 6>
-                            <<<g, 256, 0, s>>>(n, scaling, theta2, theta2d, psort, rec_c, rec_t,
-                                               agg, rope, order, f, status);
+                        launch_k(pdl, k_traverse_deferred<R, false, sizeof(R) == 4 ? 8 : 6>,
+                                 dim3(g), dim3(256), 0, s, n, scaling, theta2, theta2d, psort,
+                                 rec_c, rec_t, agg, rope, order, f, status);
                 }
             } else if (walk == WALK_PAIR) {
                 const int grid = ceil_div(ceil_div(n, 2), 256);
@@ -588,9 +595,8 @@ template <class R> struct Layout : LayoutBase {
         // with a tree, the bounding box's block count (its partials); else
         // one thread per node
         const int nb = bbox_partial ? nbbox : ceil_div(n, 256);
-        k_apply<R><<<nb, 256, 0, s>>>(n, adjust, f, fold, sw, fixed, pos, st, status,
-                                      bbox_partial, bbox, quant,
-                                      (unsigned *) (status + ST_TICKET_BBOX));
+        launch_k(pdl, k_apply<R>, dim3(nb), dim3(256), 0, s, n, adjust, f, fold, sw, fixed, pos,
+                 st, status, bbox_partial, bbox, quant, (unsigned *) (status + ST_TICKET_BBOX));
     }
     void launch_repel()
     {
@@ -885,6 +891,11 @@ template <class R> struct Layout : LayoutBase {
                 return 1;
             }
             overlap = (int) value;
+            return recapture();
+        }
+        if (!strcmp(name, "pdl") && (value == 0 || value == 1)) {
+            pdl = value == 1;
+            ss.pdl = pdl;
             return recapture();
         }
         if (!strcmp(name, "join_blocks") && value >= 1 && value <= 1 << 20) {

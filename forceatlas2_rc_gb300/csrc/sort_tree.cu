@@ -87,6 +87,7 @@ k_sort_onesweep(int n, int pass, const uint32_t *__restrict__ kin,
 
     const int shift = 8 * pass;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    pdl_wait();
     if (threadIdx.x == 0) tile_s = (int) atomicAdd(aux + SORT_AUX_TICKET + pass, 1u);
     for (int d = threadIdx.x; d < NW * 256; d += T) dsm[d] = 0;
     __syncthreads();
@@ -249,8 +250,8 @@ static void onesweep_pass(cudaStream_t s, int n, int pass, const uint32_t *kin,
                           const SortScratch &w)
 {
     const int nb = ceil_div(n, T * SORT_ITEMS);
-    k_sort_onesweep<T><<<nb, T, onesweep_smem<T>(), s>>>(
-        n, pass, kin, vin, kout, vout, w.counts + (size_t) pass * 256 * nb, w.digit_total, w.err);
+    launch_k(w.pdl, k_sort_onesweep<T>, dim3(nb), dim3(T), onesweep_smem<T>(), s, n, pass, kin,
+             vin, kout, vout, w.counts + (size_t) pass * 256 * nb, w.digit_total, w.err);
 }
 
 __global__ void __launch_bounds__(1024)

@@ -32,6 +32,7 @@ struct SortScratch {
     uint32_t *digit_total = nullptr;             // SORT_AUX
     int *err = nullptr;
     int tile_threads = 1024; // threads of a scatter block (tile = 8 keys each)
+    bool pdl = false;        // scatter passes launched as programmatic dependents
 };
 size_t sort_scratch_counts(int n); // entries of `counts`
 

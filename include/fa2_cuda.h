@@ -107,7 +107,11 @@ int fa2cu_layout_traversal_counts(fa2cu_layout *L, double counts[2]);
  *   "attract_grid" blocks per SM of that attraction, 1 (default) to 8;
  *   "join_blocks"  blocks of 256 threads of the join that adds it to the
  *                  repulsion and sums the swing totals (default 608: few
- *                  block partials for its last block). */
+ *                  block partials for its last block);
+ *   "pdl"          1: the iteration's kernels on the main stream launched
+ *                  as programmatic dependents (each is scheduled as its
+ *                  predecessor finishes; default below 500,000 nodes), 0:
+ *                  ordinary launches (identical results). */
 int fa2cu_layout_option(fa2cu_layout *L, const char *name, double value);
 
 /* A figure of the layout, by name: "launches_per_iteration" (kernels of one
