@@ -463,6 +463,7 @@ template <class R> struct Layout : LayoutBase {
     {
         launch_k(pdl, k_gather_karras<R>, dim3(ceil_div(n, 256)), dim3(256), 0, s, n, adjust,
                  order, pos, mass, size, psort, key, child, range, parent, rope, visits, status);
+        // every climb kernel waits for its predecessor before reading the tree
         switch (climb_mode) {
         case 2:
             launch_k(pdl, k_aggregate_multi<R, 2, true>, dim3(ceil_div(n, 512)), dim3(256), 0, s,
@@ -470,25 +471,28 @@ template <class R> struct Layout : LayoutBase {
                      status);
             break;
         case 4:
-            k_aggregate_multi<R, 4, true><<<ceil_div(n, 1024), 256, 0, s>>>(
-                n, psort, child, parent, range, rope, visits, agg, rec_c, rec_t, wscale, status);
+            launch_k(pdl, k_aggregate_multi<R, 4, true>, dim3(ceil_div(n, 1024)), dim3(256), 0,
+                     s, n, psort, child, parent, range, rope, visits, agg, rec_c, rec_t, wscale,
+                     status);
             break;
         case 8:
-            k_aggregate_multi<R, 8, true><<<ceil_div(n, 2048), 256, 0, s>>>(
-                n, psort, child, parent, range, rope, visits, agg, rec_c, rec_t, wscale, status);
+            launch_k(pdl, k_aggregate_multi<R, 8, true>, dim3(ceil_div(n, 2048)), dim3(256), 0,
+                     s, n, psort, child, parent, range, rope, visits, agg, rec_c, rec_t, wscale,
+                     status);
             break;
         case -2:
-            k_aggregate_multi<R, 2, false><<<ceil_div(n, 512), 256, 0, s>>>(
-                n, psort, child, parent, range, rope, visits, agg, rec_c, rec_t, wscale, status);
+            launch_k(pdl, k_aggregate_multi<R, 2, false>, dim3(ceil_div(n, 512)), dim3(256), 0,
+                     s, n, psort, child, parent, range, rope, visits, agg, rec_c, rec_t, wscale,
+                     status);
             break;
         case -4:
-            k_aggregate_multi<R, 4, false><<<ceil_div(n, 1024), 256, 0, s>>>(
-                n, psort, child, parent, range, rope, visits, agg, rec_c, rec_t, wscale, status);
+            launch_k(pdl, k_aggregate_multi<R, 4, false>, dim3(ceil_div(n, 1024)), dim3(256), 0,
+                     s, n, psort, child, parent, range, rope, visits, agg, rec_c, rec_t, wscale,
+                     status);
             break;
         default:
-            k_aggregate<R><<<ceil_div(n, 256), 256, 0, s>>>(n, psort, child, parent, range,
-                                                            rope, visits, agg, rec_c, rec_t,
-                                                            wscale, status);
+            launch_k(pdl, k_aggregate<R>, dim3(ceil_div(n, 256)), dim3(256), 0, s, n, psort,
+                     child, parent, range, rope, visits, agg, rec_c, rec_t, wscale, status);
         }
     }
     void launch_repulsion()
@@ -515,20 +519,21 @@ template <class R> struct Layout : LayoutBase {
             } else if (walk == WALK_DEFERRED) {
                 // graphs with hubs: their walks add up with compensation
                 const int g = ceil_div(n, 256);
+                // (every deferred walk waits for its predecessor first)
                 if (adjust) {
                     if (nheavy > 0)
-                        k_traverse_deferred<R, true, 6, true><<<g, 256, 0, s>>>(
-                            n, scaling, theta2, theta2d, psort, rec_c, rec_t, agg, rope, order, f,
-                            status);
+                        launch_k(pdl, k_traverse_deferred<R, true, 6, true>, dim3(g), dim3(256),
+                                 0, s, n, scaling, theta2, theta2d, psort, rec_c, rec_t, agg,
+                                 rope, order, f, status);
                     else
-                        k_traverse_deferred<R, true, 6><<<g, 256, 0, s>>>(
-                            n, scaling, theta2, theta2d, psort, rec_c, rec_t, agg, rope, order, f,
-                            status);
+                        launch_k(pdl, k_traverse_deferred<R, true, 6>, dim3(g), dim3(256), 0, s,
+                                 n, scaling, theta2, theta2d, psort, rec_c, rec_t, agg, rope,
+                                 order, f, status);
                 } else {
                     if (nheavy > 0)
-                        k_traverse_deferred<R, false, sizeof(R) == 4 ? 8 : 6, true>
-                            <<<g, 256, 0, s>>>(n, scaling, theta2, theta2d, psort, rec_c, rec_t,
-                                               agg, rope, order, f, status);
+                        launch_k(pdl, k_traverse_deferred<R, false, sizeof(R) == 4 ? 8 : 6, true>,
+                                 dim3(g), dim3(256), 0, s, n, scaling, theta2, theta2d, psort,
+                                 rec_c, rec_t, agg, rope, order, f, status);
                     else
                         launch_k(pdl, k_traverse_deferred<R, false, sizeof(R) == 4 ? 8 : 6>,
                                  dim3(g), dim3(256), 0, s, n, scaling, theta2, theta2d, psort,
