@@ -147,8 +147,8 @@ template <class R> struct Layout : LayoutBase {
     int join_blocks = 152 * 4;
     // the iteration's kernels on the main stream launched as programmatic
     // dependents (launch_k; option "pdl"), below 500,000 nodes: ms an
-    // iteration without / with, SBM 10^4 0.1431 / 0.1415, BA 10^5 0.2028 /
-    // 0.2004, SBM 10^6 0.6799 / 0.6855 (positions identical)
+    // iteration without / with, SBM 10^4 0.1435 / 0.1411, BA 10^5 0.2018 /
+    // 0.1988, SBM 10^6 0.6799 / 0.6855 (positions identical)
     bool pdl = false;
     cudaStream_t s2 = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
