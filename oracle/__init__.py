@@ -22,19 +22,26 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "_build", "libfa2oracle.so")
 REF_LIB = os.path.join(HERE, "_ref", "libfa2ref.so")
 REF_CUDA_LIB = os.path.join(HERE, "_ref", "libfa2ref_cuda.so")
-# the reference checkout (where present): FA2_REF in the environment, else
-# where this container keeps it; the GPU host has none
-REF_SRC = os.environ.get("FA2_REF") or "/root/reference"
+# the reference checkout, where one is present: FA2_REF in the environment
+# or the ref_src given to build() (no default: the GPU host has none)
+REF_SRC = os.environ.get("FA2_REF", "")
 
 
-def build(ref: bool = False, quiet: bool = True) -> None:
-    """Compile the oracle (and the reference harness when asked and its
-    sources are present) with oracle/Makefile."""
+def build(ref: bool = False, quiet: bool = True, ref_src: str = "") -> None:
+    """Compile the oracle, and when asked and the reference's sources are
+    at ref_src (or FA2_REF) the reference harness (oracle/_ref/libfa2ref.so)
+    and, if libfa2cuda.so is built, the reference's .Call layer linked
+    against it (libfa2ref_cuda.so), with oracle/Makefile."""
     out = subprocess.DEVNULL if quiet else None
     subprocess.run(["make", "-C", HERE, "-s"], check=True, stdout=out)
-    if ref and os.path.isdir(os.path.join(REF_SRC, "src")):
-        subprocess.run(["make", "-C", HERE, "-s", "ref", f"REF={REF_SRC}"], check=True,
+    src = ref_src or REF_SRC
+    if ref and src and os.path.isdir(os.path.join(src, "src")):
+        subprocess.run(["make", "-C", HERE, "-s", "ref", f"REF={src}"], check=True,
                        stdout=out)
+        cuda = os.path.join(os.path.dirname(HERE), "forceatlas2_rc_gb300", "libfa2cuda.so")
+        if os.path.exists(cuda):
+            subprocess.run(["make", "-C", HERE, "-s", "ref-cuda", f"REF={src}"], check=True,
+                           stdout=out)
 
 
 class OrcOpts(C.Structure):

@@ -56,7 +56,7 @@ def opts(d, bh=False, theta=None, threads=1):
 
 
 def main():
-    O.build(ref=True)
+    O.build(ref=True, ref_src=os.environ.get("FA2_REF", "/root/reference"))
     if O.ref_lib() is None:
         raise SystemExit("the reference could not be built (no checkout?)")
     out = {}

@@ -58,7 +58,8 @@ def cases():
 
 
 def main():
-    subprocess.run(["make", "-C", os.path.join(ROOT, "oracle"), "-s", "ref-capture"],
+    subprocess.run(["make", "-C", os.path.join(ROOT, "oracle"), "-s", "ref-capture",
+                    "REF=" + os.environ.get("FA2_REF", "/root/reference")],
                    check=True)
     lib = C.CDLL(os.path.join(ROOT, "oracle", "_ref", "libfa2ref_capture.so"))
     lib.ref_error.restype = C.c_char_p
