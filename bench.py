@@ -739,6 +739,20 @@ def batch_result(args, local, work, full=False):
     loop_s = time.perf_counter() - t0
     loop_value = len(pick) / loop_s
     loop_nodes = sum(gs[i].n for i in pick)
+    # per-step force error of the batched engine, FP32 against FP64, on the
+    # same sample (one iteration from identical float-representable
+    # positions, the forces the batch kept: fa2cu_batch_forces)
+    sub_g = [gs[i] for i in pick]
+    sub_p = [np.asarray(ps[i]).astype(np.float32).astype(np.float64) for i in pick]
+    fe = {}
+    for prec in ("single", "double"):
+        with Batch(sub_g, sub_p, precision=prec, device=local,
+                   exact_below=tuned["exact_below"], threads=tuned["threads"],
+                   nodes_per_thread=tuned["nodes_per_thread"], **kw) as Bf:
+            Bf.iterate(1)
+            Bf.sync()
+            fe[prec] = [Bf.forces(k) for k in range(len(sub_g))]
+    errs = [_rel_err(a, b) for a, b in zip(fe["single"], fe["double"])]
     return {
         "workload": BATCH_WORKLOAD if not args.small else f"{count} graphs (small check)",
         "value": value, "unit": "layouts/s", "steps": steps, "ms_per_step": ms / steps,
@@ -756,6 +770,12 @@ def batch_result(args, local, work, full=False):
             "node_iters_per_s": loop_nodes * iters / loop_s},
         "batched_over_loop": value / loop_value,
         "batched_e2e_over_loop": (count / e2e_s) / loop_value,
+        "force_err_fp32_vs_fp64": max(errs),
+        "force_err_fp32_vs_fp64_median": float(np.median(errs)),
+        "force_err_sample": f"the batched engine's forces of one iteration, FP32 against "
+                            f"FP64 from identical positions, on the {len(pick)} graphs of "
+                            f"the loop's sample (largest and median of the per-graph "
+                            f"norm-wise errors)",
         "gpu_launches": steps, "autotune_s": tune_s,
         "l2": "working set > 129 MB L2 (no flush needed)",
         "clocks": clk.summary(),
@@ -940,6 +960,24 @@ def serve_result(args, local, work, full=False):
                        i["g"].inc_coef.nbytes + 32 * i["g"].n for i in inputs])),
                    "d2h_bytes_per_step": int(np.mean([16 * i["g"].n for i in inputs])),
                    "step": "one job: submit (host arrays) to collected positions"}}
+    # per-step force error of the served layouts (the server runs Layout
+    # sessions), FP32 against FP64 from identical positions, on the first
+    # Barabasi-Albert and the first SBM job of the trace with their settings
+    from forceatlas2_rc_gb300.layout import Layout
+    ferr = {}
+    for kind in ("ba", "sbm"):
+        i = next((k for k, j in enumerate(jobs) if j["kind"] == kind), None)
+        if i is None:
+            continue
+        inp = inputs[i]
+        pos32 = np.asarray(inp["pos"]).astype(np.float32).astype(np.float64)
+        fs = {}
+        for prec in ("single", "double"):
+            with Layout(inp["g"], pos32, precision=prec, device=local, **inp["kw"]) as L:
+                fs[prec] = L.forces(pos32)
+        ferr[f"{kind} n={inp['g'].n}"] = _rel_err(fs["single"], fs["double"])
+    out["force_err_fp32_vs_fp64"] = max(ferr.values()) if ferr else None
+    out["force_err_jobs"] = ferr
     if full:
         out["at_200_per_s_least_work_first"] = serve_pass(jobs, inputs, times, local,
                                                           resident, "least_work")

@@ -77,6 +77,7 @@ def load(build_if_missing: bool = False):
         "fa2cu_batch_iterate": (C.c_int, [C.c_void_p, C.c_int]),
         "fa2cu_batch_sync": (C.c_int, [C.c_void_p]),
         "fa2cu_batch_positions": (C.c_int, [C.c_void_p, C.c_int, P_D]),
+        "fa2cu_batch_forces": (C.c_int, [C.c_void_p, C.c_int, P_D]),
         "fa2cu_batch_speed": (C.c_int, [C.c_void_p, C.c_int, P_D]),
         "fa2cu_batch_stream": (C.c_void_p, [C.c_void_p]),
         "fa2cu_batch_phase_cycles": (C.c_int, [C.c_void_p, C.c_int, P_D]),
@@ -128,7 +129,7 @@ EXPORTED = (
     "fa2cu_layout_bytes",
     "fa2cu_layout_close", "fa2cu_build_info", "fa2cu_morton_order_noalloc",
     "fa2cu_noalloc_status",
-    "fa2cu_batch_open", "fa2cu_batch_iterate", "fa2cu_batch_sync",
+    "fa2cu_batch_open", "fa2cu_batch_iterate", "fa2cu_batch_sync", "fa2cu_batch_forces",
     "fa2cu_batch_positions", "fa2cu_batch_speed", "fa2cu_batch_stream",
     "fa2cu_batch_phase_cycles",
     "fa2cu_batch_bytes", "fa2cu_batch_close", "fa2cu_batch_tune",

@@ -113,6 +113,14 @@ class Batch:
         self._check(self.lib.fa2cu_batch_positions(self.h, int(g), dptr(xy)))
         return xy.reshape(2, n).T.copy()
 
+    def forces(self, g: int) -> np.ndarray:
+        """Graph g's forces of the last iteration, at the positions before
+        its displacement, as an (n, 2) array (after ``sync``)."""
+        n = self.sizes[g]
+        f = np.zeros(2 * n)
+        self._check(self.lib.fa2cu_batch_forces(self.h, int(g), dptr(f)))
+        return f.reshape(2, n).T.copy()
+
     def speed(self, g: int) -> dict:
         st = np.zeros(4)
         self._check(self.lib.fa2cu_batch_speed(self.h, int(g), dptr(st)))

@@ -459,6 +459,7 @@ int fa2cu_batch_iterate(fa2cu_batch *B, int iterations)
 }
 int fa2cu_batch_sync(fa2cu_batch *B) { return B->impl->sync(); }
 int fa2cu_batch_positions(fa2cu_batch *B, int g, double *pos) { return B->impl->positions(g, pos); }
+int fa2cu_batch_forces(fa2cu_batch *B, int g, double *f) { return B->impl->forces(g, f); }
 int fa2cu_batch_speed(fa2cu_batch *B, int g, double state[4]) { return B->impl->speed(g, state); }
 void *fa2cu_batch_stream(fa2cu_batch *B) { return (void *) B->impl->stream(); }
 int fa2cu_batch_phase_cycles(fa2cu_batch *B, int iterations, double cycles[8])

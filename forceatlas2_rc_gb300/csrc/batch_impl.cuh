@@ -759,6 +759,27 @@ template <class R> struct Batch : BatchBase {
         return 0;
     }
 
+    // Graph g's forces of the last iteration (at the positions before its
+    // displacement): the move keeps them in f.
+    int forces(int g, double *out) override
+    {
+        if (g < 0 || g >= G) {
+            set_message("there is no graph %d in this batch", g + 1);
+            return 1;
+        }
+        cudaSetDevice(device);
+        const int n = nsize[g];
+        std::vector<R2> h((size_t) n);
+        FA2_TRY(cudaMemcpyAsync(h.data(), A.f + node0[g], (size_t) n * sizeof(R2),
+                                cudaMemcpyDeviceToHost, s),
+                "could not fetch the forces from the device", 1);
+        FA2_TRY(cudaStreamSynchronize(s), "could not fetch the forces from the device", 1);
+        for (int i = 0; i < n; i++) {
+            out[i] = (double) h[i].x;
+            out[n + i] = (double) h[i].y;
+        }
+        return 0;
+    }
     int speed(int g, double state[4]) override
     {
         if (g < 0 || g >= G) {

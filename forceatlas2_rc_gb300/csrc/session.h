@@ -79,6 +79,7 @@ struct BatchBase {
     virtual int iterate(int iterations) = 0;
     virtual int sync() = 0;
     virtual int positions(int g, double *pos) = 0;
+    virtual int forces(int g, double *f) = 0;
     virtual int speed(int g, double state[4]) = 0;
     virtual cudaStream_t stream() = 0;
     virtual double bytes() const = 0;

@@ -188,6 +188,9 @@ int fa2cu_batch_iterate(fa2cu_batch *B, int iterations);
 int fa2cu_batch_sync(fa2cu_batch *B);
 /* Positions of graph g (x then y). */
 int fa2cu_batch_positions(fa2cu_batch *B, int g, double *pos);
+/* Forces of graph g in the last iteration, at the positions before its
+ * displacement (fx then fy); after a sync. */
+int fa2cu_batch_forces(fa2cu_batch *B, int g, double *f);
 /* Speed, efficiency and last swing / traction totals of graph g. */
 int fa2cu_batch_speed(fa2cu_batch *B, int g, double state[4]);
 void *fa2cu_batch_stream(fa2cu_batch *B);

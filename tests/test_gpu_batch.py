@@ -10,11 +10,14 @@ Bars:
     summed in another fixed order);
   - FP32: after one iteration within 1e-4 (norm-wise, relative to the largest
     displacement) of the single-graph FP32 layout;
+  - one iteration's forces (fa2cu_batch_forces): FP64 within 1e-12 of the
+    oracle's, FP32 within 1e-4 of FP64;
   - a graph's positions are bit-identical alone and in any mix of graphs.
 """
 import numpy as np
 import pytest
 
+from conftest import rel_err
 from forceatlas2_rc_gb300 import graphs as G
 from forceatlas2_rc_gb300.batch import Batch, tune
 from forceatlas2_rc_gb300.layout import REPULSION_BH, REPULSION_EXACT, Graph, Layout
@@ -263,3 +266,35 @@ def test_batch_matches_oracle(gpu, orc):
         for iters, got in ((1, one[i]), (5, five[i])):
             p, keep = orc.full_params(go, iterations=iters, **kw)
             close(got, orc.pipe_run(p, pos, "d"), f"Barnes-Hut n={n}, {iters} iterations")
+
+
+def test_batch_forces_fp32_vs_fp64_and_oracle(gpu, orc):
+    """The forces of one batched iteration (fa2cu_batch_forces) from
+    identical positions: FP64 against the oracle's restatement of the
+    reference -- C_forceatlas2's exact forces for graphs below the crossover,
+    the all-GPU pipeline's Barnes-Hut forces above it -- within 1e-12, and
+    FP32 against FP64 within 1e-4 (the per-step force error of config 4)."""
+    raw = []
+    for i, n in enumerate([60, 400, 1500, 4000]):
+        n, a, b = G.erdos_renyi(n, 6.0, seed=400 + i)
+        w = np.random.default_rng(400 + i).lognormal(0.0, 0.5, len(a))
+        pos = f32(G.uniform_positions(n, -10 * np.sqrt(n), 10 * np.sqrt(n), seed=500 + i))
+        raw.append((n, a, b, w, pos))
+    gs = [Graph(n, a, b, w) for n, a, b, w, _ in raw]
+    ps = [pos for *_, pos in raw]
+    got = {}
+    for prec in ("single", "double"):
+        with Batch(gs, ps, precision=prec, exact_below=1000, threads=512,
+                   scaling=2.0, gravity=1.0, theta=1.2) as B:
+            B.iterate(1)
+            B.sync()
+            got[prec] = [B.forces(i) for i in range(len(gs))]
+    for i, (n, a, b, w, pos) in enumerate(raw):
+        if n < 1000:
+            want = orc.forces(n, a, b, w, pos, None, orc.Opts(scaling=2.0, gravity=1.0))
+        else:
+            go = orc.prepare_large(n, a, b, w)
+            p, keep = orc.full_params(go, theta=1.2, scaling=2.0, gravity=1.0)
+            want = orc.pipe_forces(p, pos, "d")
+        assert rel_err(got["double"][i], want) <= 1e-12, (n, "double")
+        assert rel_err(got["single"][i], got["double"][i]) <= 1e-4, (n, "single")
