@@ -535,3 +535,28 @@ def test_attraction_beside_the_walk(gpu, orc, opts):
     assert rel_err(fused[0], base[0]) <= 1e-6
     ext = np.abs(base[1]).max()
     assert np.abs(fused[1] - base[1]).max() <= 1e-6 * ext
+
+
+def test_layout_options_where_they_apply(gpu):
+    """The attraction beside the walk exists in single precision with the
+    Barnes-Hut repulsion only: the option is refused with a message
+    elsewhere. Programmatic dependent launches (option "pdl") change no bit
+    of a trajectory."""
+    n, a, b = G.barabasi_albert(5000, 3, seed=51)
+    w = np.ones(len(a))
+    pos = f32(G.uniform_positions(n, 0, 1000, seed=52))
+    with make_layout(n, a, b, w, pos, "double", theta=1.2) as L:
+        with pytest.raises(RuntimeError, match="single precision|Barnes-Hut"):
+            L.option("overlap", 1)
+        L.option("overlap", 0)
+    with make_layout(n, a, b, w, pos, "single", repulsion=REPULSION_EXACT) as L:
+        with pytest.raises(RuntimeError, match="single precision|Barnes-Hut"):
+            L.option("overlap", 1)
+    runs = []
+    for pdl in (0, 1):
+        with make_layout(n, a, b, w, pos, "single", theta=1.2) as L:
+            L.option("pdl", pdl)
+            L.iterate(10)
+            L.sync()
+            runs.append(L.positions())
+    np.testing.assert_array_equal(runs[0], runs[1])
