@@ -50,7 +50,10 @@ int fa2cu_layout_positions(fa2cu_layout *L, double *pos);
 int fa2cu_layout_set_positions(fa2cu_layout *L, const double *pos);
 
 /* Forces of one iteration at positions pos (repulsion, gravity, attraction),
- * into f (x then y). The layout's positions are replaced by pos. */
+ * into f (x then y), added up as the layout's iteration adds them (single
+ * precision Barnes-Hut with the "overlap" option: the repulsion plus the
+ * sum of gravity and attraction; otherwise the reference's order). The
+ * layout's positions are replaced by pos. */
 int fa2cu_layout_forces(fa2cu_layout *L, const double *pos, double *f);
 
 /* Speed, speed efficiency and the last swing / traction totals (FP64). */
